@@ -1,0 +1,240 @@
+/*
+ * solaris_gb300.h - C-ABI of the GB300 force-and-integrate engine for the
+ * Solaris planetary N-body simulator.
+ *
+ * Every entry point returns an int status (SOL_OK == 0), mirroring the
+ * reference's "return 0 = OK, 1 = error" convention (Solaris/Error.h,
+ * HANDLE_RESULT in Solaris/Acceleration.cpp:24-28); the message of the last
+ * failure on the calling thread is available from sol_last_error().  No C++
+ * exception crosses this boundary.  All pointers are plain host pointers
+ * unless the name says "_device"; host pointers are borrowed for the call
+ * only.  Device buffers are owned by the context.
+ *
+ * State layout at the boundary is the reference's: y[6N] array-of-structs
+ * (x, y, z, vx, vy, vz per body), bodies sorted by BodyType with the central
+ * body at index 0 (Solaris/BodyData.h:37-42, Solaris/Simulator.cpp:449-483).
+ */
+#ifndef SOLARIS_GB300_H_
+#define SOLARIS_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum sol_status {
+  SOL_OK = 0,
+  SOL_ERR_ARG = 1,        /* invalid argument (null pointer, bad count, ...)   */
+  SOL_ERR_CUDA = 2,       /* CUDA runtime error                                */
+  SOL_ERR_NAN = 3,        /* non-finite value detected on the device          */
+  SOL_ERR_UNDERFLOW = 4,  /* step-size underflow (RungeKuttaFehlberg78.cpp:116-122) */
+  SOL_ERR_TIMEOUT = 5,    /* a bounded device wait ran out                     */
+  SOL_ERR_MAXITER = 6,    /* Dormand-Prince retry limit (DormandPrince.cpp:158-162) */
+  SOL_ERR_NOMEM = 7,      /* device allocation failed                          */
+  SOL_ERR_STATE = 8,      /* call not valid in the context's current state     */
+  SOL_ERR_ORBIT = 9       /* unbound orbit where elements are required (Ephemeris.cpp:16-21) */
+};
+
+/* ---- body classes: numeric values of BodyType (Solaris/Body.h:231-241) -- */
+enum sol_body_type {
+  SOL_UNDEFINED_BODY_TYPE = 0,
+  SOL_CENTRAL_BODY = 1,
+  SOL_GIANT_PLANET = 2,
+  SOL_ROCKY_PLANET = 3,
+  SOL_PROTO_PLANET = 4,
+  SOL_SUPER_PLANETESIMAL = 5,
+  SOL_PLANETESIMAL = 6,
+  SOL_TEST_PARTICLE = 7
+};
+
+/* MigrationType (Solaris/Body.h:252-256) */
+enum sol_migration_type { SOL_MIGRATION_NO = 0, SOL_MIGRATION_TYPE_I = 1, SOL_MIGRATION_TYPE_II = 2 };
+
+/* GasDecreaseType (Solaris/GasDecreaseType.h) */
+enum sol_gas_decrease_type { SOL_GAS_CONSTANT = 0, SOL_GAS_LINEAR = 1, SOL_GAS_EXPONENTIAL = 2 };
+
+/* IntegratorType (Solaris/IntegratorType.h) */
+enum sol_integrator_type {
+  SOL_DORMAND_PRINCE = 0,
+  SOL_RUNGE_KUTTA4 = 1,
+  SOL_RUNGE_KUTTA56 = 2, /* declared by the reference, never implemented */
+  SOL_RUNGE_KUTTA_FEHLBERG78 = 3
+};
+
+/* Pair-force arithmetic.
+ *  FP64:  plain FP64 in the reference's form: IEEE sqrt and division, no
+ *         contraction, the operation order of GravityAC
+ *         (Solaris/Acceleration.cpp:248-329).  Bit-identical to the reference
+ *         CPU build.
+ *  SPLIT: FP64 displacement and r^2; 1/r^3 from an FP32 rsqrt seed plus one
+ *         FP64 Newton correction (carried to second order in the residual);
+ *         per-tile partial sums folded with compensated two-sum.  Relative
+ *         acceleration error against FP64 well below 1e-12.               */
+enum sol_precision { SOL_PRECISION_FP64 = 0, SOL_PRECISION_SPLIT = 1 };
+
+/* Acceleration::evaluate* switches (Solaris/Acceleration.h:375-377) */
+#define SOL_EVAL_GAS_DRAG 1u
+#define SOL_EVAL_TYPE_I 2u
+#define SOL_EVAL_TYPE_II 4u
+#define SOL_EVAL_ALL 7u
+
+/* Behaviours of the reference g++ build that a faithful replacement must
+ * reproduce.  sol_gas_component_init() sets SOL_QUIRKS_REFERENCE.
+ *  INT_ABS:      abs(double) binds to int abs() (Acceleration.cpp:770 and
+ *                Ephemeris.cpp:30): |index| and the e^2 clamp use the
+ *                truncated integer value.
+ *  BC_TAU_NU:    barycentric type-II damping uses TauNu, heliocentric uses
+ *                1/TauNu (Acceleration.cpp:518 vs :754).                    */
+#define SOL_QUIRK_INT_ABS 1u
+#define SOL_QUIRK_BC_TAU_NU 2u
+#define SOL_QUIRKS_REFERENCE (SOL_QUIRK_INT_ABS | SOL_QUIRK_BC_TAU_NU)
+
+/* ---- data model --------------------------------------------------------- */
+
+/* NBodies (Solaris/NBodies.h:62-88): counts per body class. */
+typedef struct sol_nbodies {
+  int32_t central_body;
+  int32_t giant_planet;
+  int32_t rocky_planet;
+  int32_t proto_planet;
+  int32_t super_planetesimal;
+  int32_t planetesimal;
+  int32_t test_particle;
+} sol_nbodies;
+
+/* Per-body parameters of BodyData (Solaris/BodyData.h:22-35).  Arrays have
+ * total = sum of the counts entries; bodies are sorted by type.  Any of
+ * radius/density/cd/gamma_* may be NULL when no nebula is used. */
+typedef struct sol_body_data {
+  sol_nbodies n;
+  const int32_t* id;
+  const int32_t* type;
+  const int32_t* mig_type;
+  const double* mig_stop_at;
+  const double* mass;
+  const double* radius;
+  const double* density;
+  const double* cd;
+  const double* gamma_stokes;
+  const double* gamma_epstein;
+} sol_body_data;
+
+/* PowerLaw (Solaris/PowerLaw.h): c * x^index. */
+typedef struct sol_power_law {
+  double c;
+  double index;
+} sol_power_law;
+
+/* GasComponent (Solaris/GasComponent.h:251-295). */
+typedef struct sol_gas_component {
+  double alpha;
+  int32_t decrease_type; /* sol_gas_decrease_type */
+  int32_t quirks;        /* SOL_QUIRK_* bits */
+  double time_scale;
+  double t0;
+  double t1;
+  double inner_edge;
+  double mean_molecular_weight;
+  double particle_diameter;
+  sol_power_law eta;
+  sol_power_law tau;
+  sol_power_law scale_height;
+  sol_power_law density;
+  sol_power_law mean_free_path;
+} sol_gas_component;
+
+/* TimeLine subset used by the integrator drivers (Solaris/TimeLine.h). */
+typedef struct sol_time_line {
+  double time;
+  double h_next;
+  double h_did;
+} sol_time_line;
+
+/* Counters of a driver call sequence. */
+typedef struct sol_step_stats {
+  int64_t accepted;   /* steps accepted (Counter::succededStep) */
+  int64_t rejected;   /* attempts rejected by the error control */
+  int64_t evaluations;/* force evaluations */
+} sol_step_stats;
+
+/* Event kinds of Simulator::CheckEvent (Solaris/Simulator.cpp:621-735). */
+enum sol_event_kind { SOL_EVENT_EJECTION = 1, SOL_EVENT_HIT_CENTRUM = 2, SOL_EVENT_COLLISION = 3 };
+
+typedef struct sol_event {
+  int32_t kind;  /* sol_event_kind */
+  int32_t idx1;  /* body index (0 = central body for ejection / hit-centrum) */
+  int32_t idx2;  /* body index of the other body */
+  int32_t pad;
+  double distance; /* |r| for ejection / hit-centrum, NN distance for collision */
+} sol_event;
+
+typedef struct sol_ctx sol_ctx;
+
+/* ---- utilities ---------------------------------------------------------- */
+const char* sol_last_error(void);
+int sol_version(void);
+/* Fill a GasComponent with the constructor defaults of
+ * GasComponent::GasComponent() (Solaris/GasComponent.cpp:9-34), including the
+ * mean-free-path power law built from the default density. */
+int sol_gas_component_init(sol_gas_component* gas);
+
+/* ---- context: replaces `new Acceleration(type, baryCentric, &bodyData, nebula)`
+ * (Solaris/Simulator.cpp:82, Solaris/Acceleration.cpp:35-50). ------------ */
+int sol_create(const sol_body_data* bodies, const sol_gas_component* gas_or_null,
+               int32_t barycentric, int32_t device, sol_ctx** out);
+int sol_destroy(sol_ctx* ctx);
+int sol_set_precision(sol_ctx* ctx, int32_t precision);
+/* Acceleration::evaluateGasDrag / evaluateTypeIMigration / evaluateTypeIIMigration */
+int sol_set_eval_flags(sol_ctx* ctx, uint32_t flags);
+int sol_get_n_total(const sol_ctx* ctx, int32_t* n);
+
+/* Acceleration::Compute(t, y, dydt) (Solaris/Acceleration.h:19,
+ * Solaris/Acceleration.cpp:60-80) with host buffers.  rm3, nn_idx, nn_dist
+ * (N entries each) receive Acceleration::rm3 and BodyData::indexOfNN /
+ * distanceOfNN; any of them may be NULL.  Migration side effects on
+ * BodyData::migType are kept in the context (sol_get_mig_type). */
+int sol_accel_compute(sol_ctx* ctx, double t, const double* y, double* dydt,
+                      double* rm3, int32_t* nn_idx, double* nn_dist);
+int sol_get_mig_type(const sol_ctx* ctx, int32_t* mig_type);
+
+/* ---- integrators: RungeKuttaFehlberg78::Driver, RungeKutta4::Driver,
+ * DormandPrince::Driver (Solaris/RungeKuttaFehlberg78.h:22, RungeKutta4.h:15,
+ * DormandPrince.h:14).  Each call performs n_steps driver calls on the
+ * context's resident state with device-side step control and no host
+ * round trip per attempt. ---------------------------------------------- */
+int sol_set_state(sol_ctx* ctx, const double* y0);   /* host y0[6N] -> device */
+int sol_get_state(sol_ctx* ctx, double* y0);         /* device -> host y0[6N] */
+int sol_set_tolerance(sol_ctx* ctx, double epsilon); /* RKF78/DP epsilon (1e-10 by default) */
+int sol_driver(sol_ctx* ctx, int32_t integrator, sol_time_line* tl, int32_t n_steps,
+               sol_step_stats* stats);
+/* Convenience: host y0 in, host y0 out around sol_driver. */
+int sol_driver_host(sol_ctx* ctx, int32_t integrator, double* y0, sol_time_line* tl,
+                    int32_t n_steps, sol_step_stats* stats);
+/* One RKF78 attempt at fixed h from y0 (RungeKuttaFehlberg78::Step and
+ * GetErrorMax, :147-262), with the Driver's evaluate-flag protocol (:74-95). */
+int sol_rkf78_step(sol_ctx* ctx, double t, double h, const double* y0, double* y,
+                   double* error, double* error_max);
+/* Per-body outputs of the last force evaluation (rm3, NN arrays). */
+int sol_get_last_eval(sol_ctx* ctx, double* rm3, int32_t* nn_idx, double* nn_dist);
+
+/* ---- events: predicates of Simulator::CheckEvent (Solaris/Simulator.cpp:626-645,
+ * :690-729) evaluated on the device from the last force evaluation. ------ */
+int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double collision_factor,
+                     sol_event* out, int32_t capacity, int32_t* n_out);
+
+/* ---- diagnostics: Calculate::Integrals (Solaris/Calculate.cpp:43-62). --- */
+int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
+
+/* ---- measurement helpers ------------------------------------------------ */
+/* Measured FP64 fused-multiply-add throughput of this GPU in FLOP/s (FMA = 2). */
+int sol_measure_fp64_peak(int32_t device, double* flops);
+/* Number of kernels this library launched since load. */
+int sol_kernel_launch_count(int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SOLARIS_GB300_H_ */

@@ -1,0 +1,177 @@
+"""Python binding of the CPU oracle (test infrastructure only).
+
+The oracle is the checker for the GB300 kernels: tests/, __graft_entry__.smoke()
+and bench.py's CPU-baseline leg may load it; the solaris_gb300 package never
+does.  ``build()`` compiles solaris_oracle.c with -ffp-contract=off so that its
+arithmetic is the reference's on x86-64 and aarch64 alike.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from solaris_gb300 import abi
+
+ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(ORACLE_DIR, "_build")
+LIB = os.path.join(BUILD_DIR, "liboracle.so")
+SRC = os.path.join(ORACLE_DIR, "solaris_oracle.c")
+REF_DIR = os.path.join(ORACLE_DIR, "_ref")
+REF_HARNESS = os.path.join(REF_DIR, "ref_harness")
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(ORACLE_DIR, "solaris_oracle.h"))):
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-fopenmp", SRC, "-o",
+               LIB + ".tmp", "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def build_reference(ref_root: str = "/root/reference") -> bool:
+    """Compile the reference CPU build into oracle/_ref (only where the
+    reference sources exist)."""
+    if not os.path.isdir(os.path.join(ref_root, "Solaris")):
+        return False
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, f"REF={ref_root}", "-j8"], check=True)
+    return os.path.exists(REF_HARNESS)
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(LIB)
+        P = C.c_void_p
+        F, I = abi._PF64, abi._PI32
+        lib.orc_create.restype = P
+        lib.orc_create.argtypes = [C.POINTER(abi.SolBodyData), C.POINTER(abi.SolGasComponent), C.c_int32]
+        lib.orc_destroy.argtypes = [P]
+        lib.orc_n_total.restype = C.c_int32
+        lib.orc_n_total.argtypes = [P]
+        lib.orc_set_eval_flags.argtypes = [P, C.c_uint32]
+        lib.orc_set_epsilon.argtypes = [P, C.c_double]
+        lib.orc_compute.argtypes = [P, C.c_double, F, F]
+        lib.orc_get_last_eval.argtypes = [P, F, I, F]
+        lib.orc_get_mig_type.argtypes = [P, I]
+        lib.orc_rkf78_step.argtypes = [P, C.c_double, C.c_double, F, F, F, F]
+        lib.orc_driver.argtypes = [P, C.c_int32, F, C.POINTER(abi.SolTimeLine), C.c_int32,
+                                   C.POINTER(abi.SolStepStats), F, F, F]
+        lib.orc_check_events.argtypes = [P, F, C.c_double, C.c_double, C.c_double, C.POINTER(abi.SolEvent),
+                                         C.c_int32, C.POINTER(C.c_int32)]
+        lib.orc_integrals.argtypes = [P, F, F]
+        lib.orc_kepler_equation_solver.argtypes = [C.c_double, C.c_double, C.c_double, F]
+        lib.orc_calculate_phase.argtypes = [C.c_double, F, F]
+        lib.orc_calculate_orbital_element.argtypes = [C.c_double, F, F, F, C.c_int32]
+        lib.orc_gravity_ac_sample.restype = C.c_int64
+        lib.orc_gravity_ac_sample.argtypes = [P, F, C.c_int32, C.c_int32, F, C.c_int32]
+        _lib = lib
+    return _lib
+
+
+class Oracle:
+    """One reference-semantics system (Acceleration + BodyData + integrators)."""
+
+    def __init__(self, system, barycentric=None):
+        self.lib = load()
+        self.system = system
+        self.view = abi.BodyDataView(system)
+        self.gas = abi.gas_struct(system.gas) if system.gas is not None else None
+        bary = system.barycentric if barycentric is None else barycentric
+        self.h = self.lib.orc_create(C.byref(self.view.struct), C.byref(self.gas) if self.gas else None, int(bary))
+        self.n = system.n
+        self.lib.orc_set_epsilon(self.h, system.epsilon)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def set_eval_flags(self, flags):
+        self.lib.orc_set_eval_flags(self.h, flags)
+
+    def compute(self, t, y, flags=abi.EVAL_ALL):
+        self.set_eval_flags(flags)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        d = np.zeros(6 * self.n)
+        self.lib.orc_compute(self.h, t, abi.f64p(y), abi.f64p(d))
+        return d
+
+    def last_eval(self):
+        rm3, nd = np.zeros(self.n), np.zeros(self.n)
+        nn = np.zeros(self.n, np.int32)
+        self.lib.orc_get_last_eval(self.h, abi.f64p(rm3), abi.i32p(nn), abi.f64p(nd))
+        return rm3, nn, nd
+
+    def mig_type(self):
+        m = np.zeros(self.n, np.int32)
+        self.lib.orc_get_mig_type(self.h, abi.i32p(m))
+        return m
+
+    def rkf78_step(self, t, h, y0):
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        y, err, em = np.zeros(6 * self.n), np.zeros(6 * self.n), np.zeros(1)
+        self.lib.orc_rkf78_step(self.h, t, h, abi.f64p(y0), abi.f64p(y), abi.f64p(err), abi.f64p(em))
+        return y, err, float(em[0])
+
+    def driver(self, integrator, y0, t, h, n_steps):
+        y = np.array(y0, dtype=np.float64, copy=True)
+        tl = abi.SolTimeLine(t, h, 0.0)
+        st = abi.SolStepStats()
+        times, hd, hn = np.zeros(n_steps), np.zeros(n_steps), np.zeros(n_steps)
+        rc = self.lib.orc_driver(self.h, integrator, abi.f64p(y), C.byref(tl), n_steps, C.byref(st), abi.f64p(times),
+                                 abi.f64p(hd), abi.f64p(hn))
+        return dict(status=rc, y0=y, time=times, h_did=hd, h_next=hn, tl=(tl.time, tl.h_next, tl.h_did),
+                    stats=(st.accepted, st.rejected, st.evaluations))
+
+    def check_events(self, y0, ejection, hit_centrum, collision_factor, capacity=4096):
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        ev = (abi.SolEvent * capacity)()
+        n = C.c_int32(0)
+        self.lib.orc_check_events(self.h, abi.f64p(y0), ejection, hit_centrum, collision_factor, ev, capacity,
+                                  C.byref(n))
+        return [(e.kind, e.idx1, e.idx2, e.distance) for e in ev[: min(n.value, capacity)]], n.value
+
+    def integrals(self, y0):
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        out = np.zeros(16)
+        self.lib.orc_integrals(self.h, abi.f64p(y0), abi.f64p(out))
+        return out
+
+    def gravity_sample(self, y, i_begin, i_end, n_threads=1):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        d = np.zeros(6 * self.n)
+        pairs = self.lib.orc_gravity_ac_sample(self.h, abi.f64p(y), i_begin, i_end, abi.f64p(d), n_threads)
+        return d, pairs
+
+
+def kepler(e, m, eps=1e-14):
+    lib = load()
+    E = np.zeros(1)
+    rc = lib.orc_kepler_equation_solver(e, m, eps, abi.f64p(E))
+    return rc, float(E[0])
+
+
+def calculate_phase(mu, elements):
+    lib = load()
+    el = np.ascontiguousarray(elements, dtype=np.float64)
+    ph = np.zeros(6)
+    rc = lib.orc_calculate_phase(mu, abi.f64p(el), abi.f64p(ph))
+    return rc, ph
+
+
+def orbital_element(mu, phase, quirks=abi.QUIRKS_REFERENCE):
+    lib = load()
+    ph = np.ascontiguousarray(phase, dtype=np.float64)
+    a, e = np.zeros(1), np.zeros(1)
+    rc = lib.orc_calculate_orbital_element(mu, abi.f64p(ph), abi.f64p(a), abi.f64p(e), quirks)
+    return rc, float(a[0]), float(e[0])
