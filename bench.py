@@ -1,0 +1,287 @@
+#!/usr/bin/env python
+"""Headline benchmark: pair interactions per second of the force-and-integrate
+path, split precision (<= 1e-12 relative acceleration error) beside plain FP64.
+
+Workload: 1 star + 65,535 self-gravitating bodies (equal mass 1e-10 Msun,
+a ~ U(0.5, 5) AU, e, i Rayleigh 0.02), seeded synthetic; one step is one
+RungeKutta4 driver call = 4 force evaluations of 65,535 x 65,534 direct pairs
+plus the Kepler terms, and the RK4 stage sums, all on the device.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  With N > 1 (torchrun) every rank integrates
+its own replica of the system (independent systems have no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pair interactions/s, FP64 vs split-precision at <=1e-12 rel. accel error"
+UNIT = "pair interactions/s"
+FLOP_PER_PAIR = 20  # conventional FP64 operation count of one pair interaction
+N_BODIES = 65536
+WORKLOAD = ("1 star + 65,535 self-gravitating bodies (1e-10 Msun, a~U(0.5,5) AU, e,i Rayleigh 0.02); "
+            "one RK4 step = 4 force evaluations + stage sums")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_BODIES, help=argparse.SUPPRESS)
+    return ap.parse_args()
+
+
+# ---- clocks --------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.file.read())) if len(r) >= 9]
+        os.unlink(self.file.name)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                power.append(float(r[3]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        under = [v for v in sm if v > 0.5 * max(sm)] if sm else []
+        return {"sm_mhz": statistics.median(under) if under else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+# ---- CPU baseline ----------------------------------------------------------------
+def cpu_sample(system, n_sinks: int, threads: int):
+    """GravityAC of the oracle port on sinks [1, 1 + n_sinks) of the workload."""
+    import oracle
+    o = oracle.Oracle(system)
+    t0 = time.perf_counter()
+    _, pairs = o.gravity_sample(system.y0, 1, 1 + n_sinks, threads)
+    dt = time.perf_counter() - t0
+    return pairs / dt, pairs, dt
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle port of GravityAC, all host threads)
+    on the same workload and metric."""
+    from solaris_gb300 import replicas, scenarios
+    if rank != 0:
+        replicas.finalize()
+        return
+    s = scenarios.config3(n=args.n)
+    threads = os.cpu_count() or 1
+    n_sinks = min(s.n - 1, 4096 * threads)
+    for _ in range(max(args.warmup, 0)):
+        cpu_sample(s, min(n_sinks, 256 * threads), threads)
+    pairs_total, t_total = 0, 0.0
+    for _ in range(args.steps):
+        _, pairs, dt = cpu_sample(s, n_sinks, threads)
+        pairs_total += pairs
+        t_total += dt
+    v = pairs_total / t_total
+    sample = f"GravityAC on sinks [1, {1 + n_sinks}) x all sources per step, {threads} OpenMP threads"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_bodies": s.n, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    replicas.finalize()
+
+
+def traffic_from_profiles():
+    """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "force_split_config3.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def main():
+    args = parse()
+    from solaris_gb300 import replicas
+    rank, world, local = replicas.init()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+
+    from solaris_gb300 import abi, build, engine, scenarios
+    build.build()
+    torch.cuda.set_device(local)
+    s = scenarios.config3(n=args.n)
+    pairs_eval = s.pair_count()
+    pairs_step = 4 * pairs_eval
+    ctx = engine.Context(s, device=local, precision=abi.PRECISION_SPLIT)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    l2_flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
+
+    def run_steps(precision, k, w, sampler=None):
+        ctx.set_precision(precision)
+        ctx.set_state(s.y0)
+        tl = abi.SolTimeLine(0.0, s.h0, 0.0)
+        for _ in range(w):
+            ctx.driver(abi.RUNGE_KUTTA4, 0, 0, 1, time_line=tl)
+        e_before = ctx.integrals()[15]
+        replicas.barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.start()
+        launches0 = engine.kernel_launches()
+        ms = 0.0
+        t0 = time.perf_counter()
+        for _ in range(k):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            ctx.driver(abi.RUNGE_KUTTA4, 0, 0, 1, time_line=tl)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms += ev0.elapsed_time(ev1)
+        wall = time.perf_counter() - t0
+        launches = engine.kernel_launches() - launches0
+        torch.cuda.synchronize()
+        replicas.barrier()
+        clocks = sampler.stop() if sampler else None
+        e_after = ctx.integrals()[15]
+        ms_max = replicas.max_over_ranks(ms)
+        return dict(ms_per_step=ms_max / k, wall=wall, launches=launches, clocks=clocks,
+                    energy_drift=abs((e_after - e_before) / e_before), y=ctx.get_state())
+
+    sampler = ClockSampler(local)
+    split = run_steps(abi.PRECISION_SPLIT, args.steps, args.warmup, sampler)
+    k64 = max(2, args.steps // 3)
+    fp64 = run_steps(abi.PRECISION_FP64, k64, 1)
+
+    # accuracy of the split form against the FP64 reference form on the final state
+    ctx.set_precision(abi.PRECISION_FP64)
+    a64, *_ = ctx.accel(0.0, split["y"])
+    ctx.set_precision(abi.PRECISION_SPLIT)
+    asp, *_ = ctx.accel(0.0, split["y"])
+    A, B = asp.reshape(-1, 6)[1:, 3:], a64.reshape(-1, 6)[1:, 3:]
+    rel = np.linalg.norm(A - B, axis=1) / np.linalg.norm(B, axis=1)
+
+    # dominant kernel: the pair kernel alone, per launch, CUDA events on its stream
+    ctx.set_state(s.y0)
+    ms_launch_split = ctx.bench_force(abi.PRECISION_SPLIT, 3)
+    ms_launch_fp64 = ctx.bench_force(abi.PRECISION_FP64, 2)
+    peak = engine.fp64_peak_flops(local)
+    achieved = pairs_eval * FLOP_PER_PAIR / (ms_launch_split * 1e-3)
+
+    # end to end through the C-ABI: pinned host state in, host state out, every step
+    y_host = torch.empty(6 * s.n, dtype=torch.float64, pin_memory=True).numpy()
+    y_host[:] = s.y0
+    ctx.set_precision(abi.PRECISION_SPLIT)
+    lib = ctx.lib
+    tl = abi.SolTimeLine(0.0, s.h0, 0.0)
+    st = abi.SolStepStats()
+    import ctypes as C
+    ke = max(2, args.steps // 3)
+    lib.sol_driver_host(ctx.h, abi.RUNGE_KUTTA4, abi.f64p(y_host), C.byref(tl), 1, C.byref(st))  # warm
+    replicas.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        abi.check(lib, lib.sol_driver_host(ctx.h, abi.RUNGE_KUTTA4, abi.f64p(y_host), C.byref(tl), 1, C.byref(st)))
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0)
+
+    n_ranks = world
+    value = n_ranks * pairs_step / (split["ms_per_step"] * 1e-3)
+    value64 = n_ranks * pairs_step / (fp64["ms_per_step"] * 1e-3)
+    e2e_value = n_ranks * pairs_step * ke / e2e_s
+
+    cpu = None
+    if rank == 0:
+        n_sinks = 12288
+        v, pairs, dt = cpu_sample(s, n_sinks, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"oracle GravityAC, sinks [1, {1 + n_sinks}) x 65,535 sources ({pairs:.3e} pairs, "
+                         f"{dt:.1f} s), 1 thread"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": split["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32 (split)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_bodies": s.n, "pairs_per_eval": pairs_eval, "evals_per_step": 4,
+                   "integrator": "RungeKutta4", "precision": "split",
+                   "l2": "flushed between timed steps (256 MiB write, outside the events)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": value64, "unit": UNIT, "ms_per_step": fp64["ms_per_step"], "dtype": "f64",
+                 "kernel_ms_per_launch": ms_launch_fp64,
+                 "roofline_frac": pairs_eval * FLOP_PER_PAIR / (ms_launch_fp64 * 1e-3) / peak},
+        "split_speedup_vs_fp64": value / value64,
+        "accuracy": {"split_vs_fp64_max_rel_accel_err": float(rel.max()),
+                     "split_vs_fp64_rms_rel_accel_err": float(np.sqrt(np.mean(rel ** 2))),
+                     "bound": 1e-12, "energy_drift_split": split["energy_drift"],
+                     "energy_drift_fp64": fp64["energy_drift"],
+                     "energy_drift_steps": [args.steps, k64]},
+        "roofline": {"bound": "fp64", "kernel": "k_gravity_ac<SPLIT>", "achieved": achieved / 1e12,
+                     "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": traffic_from_profiles(), "flop_per_pair": FLOP_PER_PAIR,
+                     "kernel_ms_per_launch": ms_launch_split,
+                     "peak_source": "measured in-run: FP64 FMA throughput microbenchmark (sol_measure_fp64_peak)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * 6 * s.n, "d2h_bytes_per_step": 8 * 6 * s.n,
+                "steps": ke, "api": "sol_driver_host (pinned host y0 in/out)"},
+        "gpu_launches": split["launches"],
+        "clocks": split["clocks"],
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    replicas.finalize()
+
+
+if __name__ == "__main__":
+    main()

@@ -232,6 +232,12 @@ int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
 int sol_measure_fp64_peak(int32_t device, double* flops);
 /* Number of kernels this library launched since load. */
 int sol_kernel_launch_count(int64_t* count);
+/* The CUDA stream (cudaStream_t) every kernel of this context is launched on. */
+int sol_get_stream(sol_ctx* ctx, void** stream);
+/* Average duration in milliseconds of one launch of the pair kernel alone
+ * (no prepass), over `reps` launches on the context's resident state, timed
+ * with CUDA events on the context's stream. */
+int sol_bench_force(sol_ctx* ctx, int32_t precision, int32_t reps, double* ms_per_launch);
 
 #ifdef __cplusplus
 }

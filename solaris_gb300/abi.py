@@ -176,6 +176,8 @@ def _declare(lib):
         "sol_integrals": (C.c_int, [P, _PF64, _PF64]),
         "sol_measure_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
         "sol_kernel_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
+        "sol_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
+        "sol_bench_force": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -191,7 +193,7 @@ def exported_names():
         "sol_set_precision", "sol_set_eval_flags", "sol_get_n_total", "sol_accel_compute", "sol_get_mig_type",
         "sol_set_state", "sol_get_state", "sol_set_tolerance", "sol_driver", "sol_driver_host",
         "sol_rkf78_step", "sol_get_last_eval", "sol_check_events", "sol_integrals", "sol_measure_fp64_peak",
-        "sol_kernel_launch_count"]
+        "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force"]
 
 
 def load_library(path: str | None = None):

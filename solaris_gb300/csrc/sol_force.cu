@@ -1,0 +1,472 @@
+// Force evaluation: the GB300 replacement of Acceleration::Compute
+// (Solaris/Acceleration.cpp:60-246) and its gravity, gas-drag and migration
+// terms.
+//
+// One evaluation is three launches:
+//   k_prepass     one thread per body: rm3[j] = 1/|r_j|^3 exactly as
+//                 GravityAC computes it (:256-264), and the structure-of-arrays
+//                 source table {x, y, z, G m, x rm3, y rm3, z rm3} that the pair
+//                 kernel streams; per-block partial sums of the indirect term.
+//   k_ind_reduce  one block: the indirect-term totals (SPLIT only).
+//   k_gravity_*   one thread per sink body; source tiles of TJ bodies are
+//                 staged in shared memory by bulk copies (cp.async.bulk, the
+//                 TMA engine) completing on an mbarrier, double buffered.  The
+//                 epilogue adds gas drag and type-I/II migration for the sink.
+#include <cstdio>
+
+#include "sol_internal.cuh"
+
+namespace {
+
+constexpr int kSinkBlock = 128;  // sinks per CTA
+constexpr int kTile = 256;       // sources per shared-memory tile
+constexpr int kPrepassBlock = 256;
+
+enum SrcArray { SX = 0, SY, SZ, SGM, SPX, SPY, SPZ, SRC_ARRAYS = 8 };
+
+__device__ __forceinline__ double eval_time(const TimeSpec& ts) {
+  return ts.base ? (*ts.base + ts.c * (*ts.h)) : ts.t_host;
+}
+
+// ---- prepass ----------------------------------------------------------------
+__global__ void k_prepass(ForceCtx fc, const double* __restrict__ y, int split) {
+  const int n = fc.cls.n;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double q[6] = {0, 0, 0, 0, 0, 0};  // indirect contributions: massive range, super-planetesimal range
+  if (j < fc.npad) {
+    double x = 0, yy = 0, z = 0, gm = 0, px = 0, py = 0, pz = 0;
+    if (j < n) {
+      x = y[6 * j + 0];
+      yy = y[6 * j + 1];
+      z = y[6 * j + 2];
+      double rm3 = 0.0;
+      if (j >= 1) {
+        if (!fc.barycentric) {
+          // Acceleration.cpp:259-261
+          double r2 = x * x + yy * yy + z * z;
+          double r = __dsqrt_rn(r2);
+          rm3 = __ddiv_rn(1.0, r2 * r);
+          fc.rm3[j] = rm3;
+        }
+        gm = SOL_GAUSS2 * fc.mass[j];
+      }
+      px = x * rm3;
+      py = yy * rm3;
+      pz = z * rm3;
+      if (fc.barycentric) gm = fc.mass[j];  // GravityBC uses m_j and scales by G at the end
+      if (split && j >= 1) {
+        int slot = (j < fc.cls.nm) ? 0 : ((j < fc.cls.nm + fc.cls.n_spl) ? 3 : -1);
+        if (slot >= 0) {
+          q[slot + 0] = gm * px;
+          q[slot + 1] = gm * py;
+          q[slot + 2] = gm * pz;
+        }
+      }
+    }
+    double* s = fc.src;
+    const int np = fc.npad;
+    s[SX * np + j] = x;
+    s[SY * np + j] = yy;
+    s[SZ * np + j] = z;
+    s[SGM * np + j] = gm;
+    s[SPX * np + j] = px;
+    s[SPY * np + j] = py;
+    s[SPZ * np + j] = pz;
+  }
+  if (!split) return;
+  // fixed-order block tree reduction of the indirect contributions
+  __shared__ double red[6][kPrepassBlock];
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = q[k];
+  __syncthreads();
+  for (int w = kPrepassBlock / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) fc.ind_part[6 * blockIdx.x + k] = red[k][0];
+}
+
+__global__ void k_ind_reduce(ForceCtx fc) {
+  // one block of 256 threads: strided partial sums then a fixed tree.
+  __shared__ double red[6][256];
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < fc.n_ind_blocks; b += blockDim.x)
+    for (int k = 0; k < 6; ++k) a[k] += fc.ind_part[6 * b + k];
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = a[k];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    // [0..2]: sum over [1, nm); [3..5]: sum over [1, nm + n_spl)
+    for (int k = 0; k < 3; ++k) {
+      fc.ind_sum[k] = red[k][0];
+      fc.ind_sum[3 + k] = red[k][0] + red[3 + k][0];
+    }
+  }
+}
+
+// ---- epilogue: drag and migration of one sink (ComputeAstroCentric :176-243) --
+__device__ __forceinline__ void add_gas_terms(const ForceCtx& fc, int i, const double* yi, double t,
+                                              uint32_t flags, double a[3]) {
+  const GasDev& g = fc.gas;
+  if (!g.present) return;
+  const Classes& c = fc.cls;
+  const double m0 = fc.mass[0];
+  const int lower_drag = c.nm, upper_drag = c.nm + c.n_spl + c.n_pl;
+  if (i >= lower_drag && i < upper_drag) {
+    double* buf = fc.drag + 3 * (i - lower_drag);
+    if (flags & SOL_EVAL_GAS_DRAG) {
+      double d[3];
+      sol_gas_drag(g, sol_reduction_factor(g, t), m0, yi, fc.radius[i], fc.density[i], fc.cd[i],
+                   fc.gamma_stokes[i], fc.gamma_epstein[i], d);
+      buf[0] = d[0];
+      buf[1] = d[1];
+      buf[2] = d[2];
+    }
+    a[0] += buf[0];
+    a[1] += buf[1];
+    a[2] += buf[2];
+    return;
+  }
+  const int lower1 = c.n_central + c.n_giant;
+  if (fc.has_mig1 && i >= lower1 && i < c.nm) {
+    double* buf = fc.mig1 + 3 * (i - lower1);
+    if ((flags & SOL_EVAL_TYPE_I) && fc.mig_type[i] == SOL_MIGRATION_TYPE_I) {
+      double d[3];
+      if (!sol_migration_type1(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
+        fc.mig_type[i] = SOL_MIGRATION_NO;
+      buf[0] = d[0];
+      buf[1] = d[1];
+      buf[2] = d[2];
+    }
+    if (fc.mig_type[i] != SOL_MIGRATION_NO) {
+      a[0] += buf[0];
+      a[1] += buf[1];
+      a[2] += buf[2];
+    }
+    return;
+  }
+  const int lower2 = c.n_central;
+  if (fc.has_mig2 && i >= lower2 && i < c.n_central + c.n_giant) {
+    double* buf = fc.mig2 + 3 * (i - lower2);
+    if ((flags & SOL_EVAL_TYPE_II) && fc.mig_type[i] == SOL_MIGRATION_TYPE_II) {
+      double d[3];
+      if (!sol_migration_type2(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
+        fc.mig_type[i] = SOL_MIGRATION_NO;
+      buf[0] = d[0];
+      buf[1] = d[1];
+      buf[2] = d[2];
+    }
+    if (fc.mig_type[i] != SOL_MIGRATION_NO) {
+      a[0] += buf[0];
+      a[1] += buf[1];
+      a[2] += buf[2];
+    }
+  }
+}
+
+// ---- tile pipeline -----------------------------------------------------------
+template <int NARR>
+struct TileSmem {
+  double v[2][NARR][kTile];
+  uint64_t bar[2];
+};
+
+template <int NARR>
+__device__ __forceinline__ void issue_tile(TileSmem<NARR>& sm, const double* src, int npad, int tile, int stage) {
+  sol_mbar_expect_tx(&sm.bar[stage], NARR * kTile * 8);
+  for (int k = 0; k < NARR; ++k)
+    sol_bulk_g2s(&sm.v[stage][k][0], src + (size_t)k * npad + (size_t)tile * kTile, kTile * 8, &sm.bar[stage]);
+}
+
+// Reference-form pair arithmetic (GravityAC, Acceleration.cpp:294-317): IEEE
+// sqrt and division, no contraction, sources in ascending order.
+__device__ __forceinline__ void pair_fp64(const TileSmem<7>& sm, int st, int jj, int j, int i, int ns, double xi,
+                                          double yi, double zi, double& ax, double& ay, double& az, long long& rminb,
+                                          int& nn) {
+  if (j >= 1 && j < ns && j != i) {
+    double xij = sm.v[st][SX][jj] - xi;
+    double yij = sm.v[st][SY][jj] - yi;
+    double zij = sm.v[st][SZ][jj] - zi;
+    double rij2 = xij * xij + yij * yij + zij * zij;
+    double rij = __dsqrt_rn(rij2);
+    double rijm3 = __ddiv_rn(1.0, rij2 * rij);
+    long long rb = __double_as_longlong(rij);
+    if (rb < rminb) {
+      rminb = rb;
+      nn = j;
+    }
+    double gm = sm.v[st][SGM][jj];
+    ax += gm * (xij * rijm3 - sm.v[st][SPX][jj]);
+    ay += gm * (yij * rijm3 - sm.v[st][SPY][jj]);
+    az += gm * (zij * rijm3 - sm.v[st][SPZ][jj]);
+  }
+}
+
+// Split pair arithmetic: FP64 displacement and r^2; rsqrt seed in FP32 with
+// the FP64 <-> FP32 conversions done by integer operations on the bit
+// patterns (they stay off the FP64 pipe); one FP64 Newton correction of
+// r^-3 carried to second order in the residual e = 1 - r^2 y0^2:
+//   r^-3 = y0^3 (1 - e)^(-3/2) = y0^3 (1 + 3/2 e + 15/8 e^2 + O(e^3)),
+// |e| < 1e-6, so the truncation is below 1e-18.  16 FP64 operations per pair.
+__device__ __forceinline__ void pair_split(const TileSmem<4>& sm, int st, int jj, int j, int i, int ns, double xi,
+                                           double yi, double zi, double& ax, double& ay, double& az,
+                                           long long& r2minb, int& nn) {
+  double dx = sm.v[st][SX][jj] - xi;
+  double dy = sm.v[st][SY][jj] - yi;
+  double dz = sm.v[st][SZ][jj] - zi;
+  double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, dz * dz));
+  // FP64 -> FP32 by truncation of the high word, clamped to the normal FP32
+  // range so that r2 == 0 (the sink itself) gives a finite seed.
+  int hi = __double2hiint(r2);
+  hi = min(max(hi, 0x38100000), 0x47EFFFFF);
+  float f = __int_as_float((hi - 0x38000000) << 3);
+  float yf = rsqrtf(f);
+  int fb = __float_as_int(yf);
+  double y0 = __hiloint2double((fb >> 3) + 0x38000000, fb << 29);
+  double u = y0 * y0;
+  double e = __fma_rn(-r2, u, 1.0);
+  double y3 = u * y0;
+  double cpoly = __fma_rn(e, 1.875, 1.5);
+  double corr = __fma_rn(e, cpoly, 1.0);
+  double gm = (j < ns) ? sm.v[st][SGM][jj] : 0.0;  // gm of j == 0 and of padding is 0
+  double s = (gm * y3) * corr;
+  ax = __fma_rn(s, dx, ax);
+  ay = __fma_rn(s, dy, ay);
+  az = __fma_rn(s, dz, az);
+  long long rb = __double_as_longlong(r2);
+  bool better = (rb < r2minb) & (j >= 1) & (j < ns) & (j != i);
+  r2minb = better ? rb : r2minb;
+  nn = better ? j : nn;
+}
+
+__device__ __forceinline__ void two_sum(double& s, double& c, double a) {
+  double t = s + a;
+  double bp = t - s;
+  double err = (s - (t - bp)) + (a - bp);
+  s = t;
+  c += err;
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const double* __restrict__ y,
+                                                           double* __restrict__ dydt, TimeSpec ts, uint32_t flags,
+                                                           int* dev_status) {
+  constexpr int NARR = (PREC == SOL_PRECISION_FP64) ? 7 : 4;
+  __shared__ __align__(128) TileSmem<NARR> sm;
+  const Classes& c = fc.cls;
+  const int n = c.n;
+  const int i = blockIdx.x * kSinkBlock + threadIdx.x;
+  const int i_first = blockIdx.x * kSinkBlock;
+  // NOfMassive of GravityAC (:285-289); types are sorted, so the first sink
+  // of the CTA has the largest source range.
+  const int ns_cta = (fc.type[min(i_first, n - 1)] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
+  const int ns = (i < n && fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
+  const int ntiles = (ns_cta + kTile - 1) / kTile;
+
+  double xi = 0, yi = 0, zi = 0;
+  if (i < n) {
+    xi = y[6 * i + 0];
+    yi = y[6 * i + 1];
+    zi = y[6 * i + 2];
+  }
+  if (threadIdx.x == 0) {
+    sol_mbar_init(&sm.bar[0], 1);
+    sol_mbar_init(&sm.bar[1], 1);
+    sol_fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (ntiles > 0) issue_tile<NARR>(sm, fc.src, fc.npad, 0, 0);
+    if (ntiles > 1) issue_tile<NARR>(sm, fc.src, fc.npad, 1, 1);
+  }
+
+  double ax = 0.0, ay = 0.0, az = 0.0;  // FP64: running sums; SPLIT: tile partials
+  double sx = 0.0, sy = 0.0, sz = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;  // SPLIT compensated totals
+  long long rminb = (PREC == SOL_PRECISION_FP64) ? __double_as_longlong(1.0e10) : __double_as_longlong(1.0e20);
+  int nn = -1;
+  int issued = ntiles < 2 ? ntiles : 2;
+  int t = 0;
+  bool timed_out = false;
+
+  for (; t < ntiles; ++t) {
+    const int st = t & 1;
+    const uint32_t parity = (t >> 1) & 1;
+    const bool ok = sol_mbar_wait(&sm.bar[st], parity);
+    const int j0 = t * kTile;
+    if (ok && i < n && i >= 1) {
+      if constexpr (PREC == SOL_PRECISION_FP64) {
+#pragma unroll 4
+        for (int jj = 0; jj < kTile; ++jj)
+          pair_fp64(*reinterpret_cast<TileSmem<7>*>(&sm), st, jj, j0 + jj, i, ns, xi, yi, zi, ax, ay, az, rminb,
+                    nn);
+      } else {
+        double tx = 0.0, ty = 0.0, tz = 0.0;
+#pragma unroll 4
+        for (int jj = 0; jj < kTile; ++jj)
+          pair_split(*reinterpret_cast<TileSmem<4>*>(&sm), st, jj, j0 + jj, i, ns, xi, yi, zi, tx, ty, tz, rminb,
+                     nn);
+        two_sum(sx, cx, tx);
+        two_sum(sy, cy, ty);
+        two_sum(sz, cz, tz);
+      }
+    }
+    // every thread is done with stage st; a timeout anywhere stops the whole CTA
+    if (__syncthreads_or(!ok)) {
+      timed_out = true;
+      break;
+    }
+    if (threadIdx.x == 0 && t + 2 < ntiles) {
+      sol_fence_proxy_async();
+      issue_tile<NARR>(sm, fc.src, fc.npad, t + 2, st);
+    }
+    if (t + 2 < ntiles) issued = t + 3;
+  }
+  if (timed_out) {
+    if (threadIdx.x == 0) {
+      atomicOr(dev_status, SOL_DEV_TIMEOUT);
+      // drain the copies still in flight (bounded) before the CTA exits
+      for (int u = t; u < issued; ++u) sol_mbar_wait(&sm.bar[u & 1], (u >> 1) & 1);
+    }
+    __syncthreads();
+    return;
+  }
+  if (i >= n) return;
+  double* out = dydt + 6 * i;
+  if (i == 0) {  // GravityAC :253-254, :266
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    fc.nn_idx[0] = -1;
+    fc.nn_dist[0] = 0.0;
+    return;
+  }
+  const double* yv = y + 6 * i;
+  const double mu = SOL_GAUSS2 * (fc.mass[0] + fc.mass[i]);
+  const double rm3i = fc.rm3[i];
+  double a[3];
+  a[0] = -mu * rm3i * xi;  // Kepler term first (:281-283)
+  a[1] = -mu * rm3i * yi;
+  a[2] = -mu * rm3i * zi;
+  if constexpr (PREC == SOL_PRECISION_FP64) {
+    a[0] += ax;
+    a[1] += ay;
+    a[2] += az;
+    fc.nn_idx[i] = nn;
+    fc.nn_dist[i] = nn >= 0 ? __longlong_as_double(rminb) : 0.0;
+  } else {
+    const double* S = fc.ind_sum + ((fc.type[i] <= SOL_PROTO_PLANET) ? 3 : 0);
+    const bool src_i = i < ns;
+    const double* s = fc.src;
+    const int np = fc.npad;
+    double own[3] = {0.0, 0.0, 0.0};
+    if (src_i) {
+      double gmi = s[SGM * np + i];
+      own[0] = gmi * s[SPX * np + i];
+      own[1] = gmi * s[SPY * np + i];
+      own[2] = gmi * s[SPZ * np + i];
+    }
+    a[0] += (sx + cx) - (S[0] - own[0]);
+    a[1] += (sy + cy) - (S[1] - own[1]);
+    a[2] += (sz + cz) - (S[2] - own[2]);
+    fc.nn_idx[i] = nn;
+    fc.nn_dist[i] = nn >= 0 ? __dsqrt_rn(__longlong_as_double(rminb)) : 0.0;
+  }
+  add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
+  out[0] = yv[3];
+  out[1] = yv[4];
+  out[2] = yv[5];
+  out[3] = a[0];
+  out[4] = a[1];
+  out[5] = a[2];
+}
+
+// GravityBC_SelfInteracting / _NonSelfInteracting (Acceleration.cpp:541-634):
+// massive sinks and non-massive sinks both sum over massive sources in
+// descending order, scale by G at the end; no rm3.
+__global__ void __launch_bounds__(kSinkBlock) k_gravity_bc(ForceCtx fc, const double* __restrict__ y,
+                                                           double* __restrict__ dydt, TimeSpec ts,
+                                                           uint32_t flags) {
+  const int n = fc.cls.n;
+  const int i = blockIdx.x * kSinkBlock + threadIdx.x;
+  if (i >= n) return;
+  const double* s = fc.src;
+  const int np = fc.npad;
+  const double* yv = y + 6 * i;
+  double xi = yv[0], yi = yv[1], zi = yv[2];
+  double a[3] = {0.0, 0.0, 0.0};
+  long long rminb = __double_as_longlong(1.0e10);
+  int nn = -1;
+  for (int j = fc.cls.nm - 1; j >= 0; j--) {
+    if (j == i) continue;
+    double dx = s[SX * np + j] - xi;
+    double dy = s[SY * np + j] - yi;
+    double dz = s[SZ * np + j] - zi;
+    double rij2 = dx * dx + dy * dy + dz * dz;
+    double rij = __dsqrt_rn(rij2);
+    long long rb = __double_as_longlong(rij);
+    if (rb < rminb) {
+      rminb = rb;
+      nn = j;
+    }
+    double cc = __ddiv_rn(s[SGM * np + j] * 1.0, rij2 * rij);
+    a[0] += cc * dx;
+    a[1] += cc * dy;
+    a[2] += cc * dz;
+  }
+  a[0] *= SOL_GAUSS2;
+  a[1] *= SOL_GAUSS2;
+  a[2] *= SOL_GAUSS2;
+  fc.nn_idx[i] = nn;
+  fc.nn_dist[i] = nn >= 0 ? __longlong_as_double(rminb) : 0.0;
+  add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
+  double* out = dydt + 6 * i;
+  out[0] = yv[3];
+  out[1] = yv[4];
+  out[2] = yv[5];
+  out[3] = a[0];
+  out[4] = a[1];
+  out[5] = a[2];
+}
+
+}  // namespace
+
+// parts: 1 = prepass (and indirect totals), 2 = pair kernel, 3 = both.
+int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int parts) {
+  ForceCtx& fc = c->fc;
+  const int split = (c->precision == SOL_PRECISION_SPLIT && !c->barycentric) ? 1 : 0;
+  if (parts & 1) {
+    const int nb_pre = (fc.npad + kPrepassBlock - 1) / kPrepassBlock;
+    k_prepass<<<nb_pre, kPrepassBlock, 0, c->stream>>>(fc, d_y, split);
+    SOL_LAUNCHED();
+    if (split && !c->barycentric) {
+      k_ind_reduce<<<1, 256, 0, c->stream>>>(fc);
+      SOL_LAUNCHED();
+    }
+  }
+  if (!(parts & 2)) return SOL_OK;
+  const int nb = (c->n + kSinkBlock - 1) / kSinkBlock;
+  if (c->barycentric) {
+    k_gravity_bc<<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
+    SOL_LAUNCHED();
+    return SOL_OK;
+  }
+  if (split) {
+    k_gravity_ac<SOL_PRECISION_SPLIT><<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags,
+                                                                        &c->d_ctrl->dev_status);
+  } else {
+    k_gravity_ac<SOL_PRECISION_FP64><<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags,
+                                                                       &c->d_ctrl->dev_status);
+  }
+  SOL_LAUNCHED();
+  return SOL_OK;
+}
+
+int sol_force_launch(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags) {
+  return sol_force_launch_parts(c, d_y, d_dydt, ts, flags, 3);
+}
+
+int sol_force_tile() { return kTile; }
+int sol_force_prepass_blocks(int npad) { return (npad + kPrepassBlock - 1) / kPrepassBlock; }

@@ -1,0 +1,559 @@
+// Integrator drivers on the device: RungeKuttaFehlberg78, RungeKutta4 and
+// DormandPrince (Solaris/RungeKuttaFehlberg78.cpp, RungeKutta4.cpp,
+// DormandPrince.cpp).
+//
+// Stage combinations, the final sums and the error estimates are streaming
+// kernels over the 6N state (read k vectors, write one) in the reference's
+// operation order, so that with the FP64 force they reproduce the reference
+// bit for bit.  The error norm is reduced on the device and the step-size
+// decision (accept / shrink / grow, underflow, retry limit) is taken by a
+// one-thread control kernel that updates the device control block; the host
+// only reads the control block to decide whether to launch another attempt.
+#include <cmath>
+#include <cstring>
+
+#include "sol_internal.cuh"
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kMaxTerms = 9;
+
+struct StageArgs {
+  const double* f[kMaxTerms];
+  double a[kMaxTerms];
+};
+
+inline int grid_for(int n) {
+  int g = (n + kBlock - 1) / kBlock;
+  return g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g);
+}
+
+// yt = y0 + h * (a0 f0 + a1 f1 + ...), summed left to right
+// (RungeKuttaFehlberg78.cpp:170-232, RungeKutta4.cpp:413-433).
+template <int K>
+__global__ void k_stage(int nv, const double* __restrict__ y0, double* __restrict__ out, StageArgs s,
+                        const sol_ctrl* ctrl) {
+  const double h = ctrl->h;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+    double acc = s.a[0] * s.f[0][i];
+#pragma unroll
+    for (int k = 1; k < K; ++k) acc = acc + s.a[k] * s.f[k][i];
+    out[i] = y0[i] + h * acc;
+  }
+}
+
+// yscale = |y0| + |h f0| + TINY (RungeKuttaFehlberg78.cpp:87-89)
+__global__ void k_yscale(int nv, const double* __restrict__ y0, const double* __restrict__ f0,
+                         double* __restrict__ ys, const sol_ctrl* ctrl) {
+  const double h = ctrl->h;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x)
+    ys[i] = fabs(y0[i]) + fabs(h * f0[i]) + 1.0e-30;
+}
+
+struct Rkf78FinalArgs {
+  const double* f[13];
+};
+
+// The 7th-order result, the error estimate and the block maxima of
+// |error / yscale| (RungeKuttaFehlberg78.cpp:236-242, :252-262).
+__global__ void k_rkf78_final(int nv, const double* __restrict__ y0, Rkf78FinalArgs fa, double* __restrict__ y,
+                              double* __restrict__ err, const double* __restrict__ ys, double* __restrict__ partial,
+                              const sol_ctrl* ctrl) {
+  const double h = ctrl->h;
+  const double D1_0 = 41.0 / 840.0, D1_5 = 34.0 / 105.0, D1_6 = 9.0 / 35.0, D1_8 = 9.0 / 280.0,
+               D1_10 = 41.0 / 840.0;
+  double m = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+    const double f0 = fa.f[0][i], f10 = fa.f[10][i];
+    y[i] = y0[i] + h * (D1_0 * f0 + D1_5 * fa.f[5][i] + D1_6 * (fa.f[6][i] + fa.f[7][i]) +
+                        D1_8 * (fa.f[8][i] + fa.f[9][i]) + D1_10 * f10);
+    double e = h * fabs(f0 + f10 - fa.f[11][i] - fa.f[12][i]) * 41.0 / 840.0;
+    err[i] = e;
+    double q = fabs(e / ys[i]);
+    m = (q > m || q != q) ? q : m;  // a NaN propagates into the norm
+  }
+  __shared__ double red[kBlock];
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = kBlock / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      double o = red[threadIdx.x + w];
+      if (o > red[threadIdx.x] || o != o) red[threadIdx.x] = o;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// max over block partials -> ctrl->error_max (divided by eps for RKF78)
+__global__ void k_reduce_max(const double* __restrict__ partial, int np, sol_ctrl* ctrl, int divide_eps) {
+  __shared__ double red[kBlock];
+  double m = 0.0;
+  for (int b = threadIdx.x; b < np; b += blockDim.x) {
+    double o = partial[b];
+    if (o > m || o != o) m = o;
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = kBlock / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      double o = red[threadIdx.x + w];
+      if (o > red[threadIdx.x] || o != o) red[threadIdx.x] = o;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ctrl->error_max = divide_eps ? red[0] / ctrl->eps : red[0];
+}
+
+// Step-size control of RungeKuttaFehlberg78::Driver (:98-133).
+__global__ void k_control_rkf78(sol_ctrl* c) {
+  const double em = c->error_max;
+  const double h = c->h;
+  if (em < 1.0) {
+    c->h_did = h;
+    c->t += c->h_did;
+    c->h_next = em > 1.89e-4 ? (0.9 * h * pow(em, -0.2)) : (5.0 * h);
+    c->h = c->h_next;
+    c->accepted = 1;
+    c->n_accepted++;
+    return;
+  }
+  c->n_rejected++;
+  if (em != em) {  // non-finite error norm: stop instead of shrinking to underflow
+    c->dev_status |= SOL_DEV_UNDERFLOW;
+    return;
+  }
+  double hTemp = 0.9 * h * pow(em, -0.25);
+  double hn = fabs(hTemp) > fabs(0.1 * h) ? hTemp : 0.1 * h;
+  c->h = hn;
+  double tNew = c->t + hn;
+  if (tNew == c->t) c->dev_status |= SOL_DEV_UNDERFLOW;
+}
+
+// RungeKutta4::Driver bookkeeping (RungeKutta4.cpp:355-365)
+__global__ void k_control_rk4(sol_ctrl* c) {
+  c->h_did = c->h;
+  c->t += c->h_did;
+  c->h_next = c->h;
+  c->accepted = 1;
+  c->n_accepted++;
+}
+
+// Begin a driver call: bodyData->h = timeLine->hNext (RungeKuttaFehlberg78.cpp:74-75)
+__global__ void k_begin_step(sol_ctrl* c) {
+  c->h = c->h_next;
+  c->accepted = 0;
+  c->iter = 0;
+}
+
+// ---- Dormand-Prince RKN 7(6), DormandPrince::Step2 (:246-491) ---------------
+struct DpStageArgs {
+  const double* f[8];
+  double a[8];
+  double ck;  // c[k]
+};
+
+template <int K>
+__global__ void k_dp_stage(int n, const double* __restrict__ y0, double* __restrict__ yt, DpStageArgs s,
+                           const sol_ctrl* ctrl) {
+  const double h = ctrl->h;
+  const double h2 = h * h;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
+    const int nn = 6 * (q / 3) + (q % 3);
+    double var = s.a[0] * s.f[0][nn + 3];
+#pragma unroll
+    for (int l = 1; l < K; ++l) var = var + s.a[l] * s.f[l][nn + 3];
+    yt[nn] = y0[nn] + s.ck * h * y0[nn + 3] + h2 * (var);
+    yt[nn + 3] = y0[nn + 3] + h * (var);
+  }
+}
+
+struct DpFinalArgs {
+  const double* f[9];
+  double b[9], bdh[9];
+};
+
+__global__ void k_dp_final(int n, const double* __restrict__ y0, DpFinalArgs s, double* __restrict__ y,
+                           double* __restrict__ err, double* __restrict__ partial, const sol_ctrl* ctrl) {
+  const double h = ctrl->h;
+  const double h2 = h * h;
+  double m = 0.0;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += gridDim.x * blockDim.x) {
+    const int nn = 6 * (q / 3) + (q % 3);
+    const double f0 = s.f[0][nn + 3], f4 = s.f[4][nn + 3], f5 = s.f[5][nn + 3], f6 = s.f[6][nn + 3],
+                 f7 = s.f[7][nn + 3], f8 = s.f[8][nn + 3];
+    y[nn] = y0[nn] + h * y0[nn + 3] +
+            h2 * (s.b[0] * f0 + s.b[4] * f4 + s.b[5] * f5 + s.b[6] * f6 + s.b[7] * f7 + s.b[8] * f8);
+    double e = h2 * fabs(f7 - f8) / 20.0;
+    err[nn] = e;
+    y[nn + 3] = y0[nn + 3] + h * (s.bdh[0] * f0 + s.bdh[4] * f4 + s.bdh[5] * f5 + s.bdh[6] * f6 + s.bdh[7] * f7);
+    err[nn + 3] = 0.0;
+    double q2 = fabs(e);
+    m = (q2 > m || q2 != q2) ? q2 : m;
+  }
+  __shared__ double red[kBlock];
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = kBlock / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      double o = red[threadIdx.x + w];
+      if (o > red[threadIdx.x] || o != o) red[threadIdx.x] = o;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+// DormandPrince::Driver loop condition and step update (:145-164)
+__global__ void k_control_dp(sol_ctrl* c) {
+  const double em = c->error_max;
+  const double h = c->h;
+  c->iter++;
+  c->h_did = h;
+  c->h_next = em < 1.0e-20 ? 2.0 * h : 0.9 * h * pow(c->eps / em, 1.0 / 7.0);
+  if (em > c->eps && c->iter <= 10) {
+    c->n_rejected++;
+    c->h = c->h_next;  // the next attempt uses timeLine->hNext
+    return;
+  }
+  if (c->iter > 10) {
+    c->dev_status |= SOL_DEV_MAXITER;
+    return;
+  }
+  c->t += c->h_did;
+  c->accepted = 1;
+  c->n_accepted++;
+}
+
+// RKF78 stage tableau (RungeKuttaFehlberg78.cpp:41-56): per stage, the k
+// indices it reads and the coefficients, in the order of the reference sums.
+struct Rkf78Stage {
+  int k;
+  int idx[kMaxTerms];
+  double a[kMaxTerms];
+};
+
+const Rkf78Stage* rkf78_stages() {
+  static Rkf78Stage st[13];
+  static bool init = false;
+  if (!init) {
+    auto set = [](Rkf78Stage& s, std::initializer_list<int> idx, std::initializer_list<double> a) {
+      s.k = (int)idx.size();
+      int p = 0;
+      for (int v : idx) s.idx[p++] = v;
+      p = 0;
+      for (double v : a) s.a[p++] = v;
+    };
+    set(st[1], {0}, {2.0 / 27.0});
+    set(st[2], {0, 1}, {1.0 / 36.0, 1.0 / 12.0});
+    set(st[3], {0, 2}, {1.0 / 24.0, 1.0 / 8.0});
+    set(st[4], {0, 2, 3}, {5.0 / 12.0, -25.0 / 16.0, 25.0 / 16.0});
+    set(st[5], {0, 3, 4}, {1.0 / 20.0, 1.0 / 4.0, 1.0 / 5.0});
+    set(st[6], {0, 3, 4, 5}, {-25.0 / 108.0, 125.0 / 108.0, -65.0 / 27.0, 125.0 / 54.0});
+    set(st[7], {0, 4, 5, 6}, {31.0 / 300.0, 61.0 / 225.0, -2.0 / 9.0, 13.0 / 900.0});
+    set(st[8], {0, 3, 4, 5, 6, 7}, {2.0, -53.0 / 6.0, 704.0 / 45.0, -107.0 / 9.0, 67.0 / 90.0, 3.0});
+    set(st[9], {0, 3, 4, 5, 6, 7, 8},
+        {-91.0 / 108.0, 23.0 / 108.0, -976.0 / 135.0, 311.0 / 54.0, -19.0 / 60.0, 17.0 / 6.0, -1.0 / 12.0});
+    set(st[10], {0, 3, 4, 5, 6, 7, 8, 9},
+        {2383.0 / 4100.0, -341.0 / 164.0, 4496.0 / 1025.0, -301.0 / 82.0, 2133.0 / 4100.0, 45.0 / 82.0,
+         45.0 / 164.0, 18.0 / 41.0});
+    set(st[11], {0, 5, 6, 7, 8, 9}, {3.0 / 205.0, -6.0 / 41.0, -3.0 / 205.0, -3.0 / 41.0, 3.0 / 41.0, 6.0 / 41.0});
+    set(st[12], {0, 3, 4, 5, 6, 7, 8, 9, 11},
+        {-1777.0 / 4100.0, -341.0 / 164.0, 4496.0 / 1025.0, -289.0 / 82.0, 2193.0 / 4100.0, 51.0 / 82.0,
+         33.0 / 164.0, 12.0 / 41.0, 1.0});
+    init = true;
+  }
+  return st;
+}
+
+int launch_stage(sol_ctx* c, int k, const StageArgs& s, const double* y0, double* out) {
+  const int g = grid_for(c->nv);
+  switch (k) {
+    case 1: k_stage<1><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    case 2: k_stage<2><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    case 3: k_stage<3><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    case 4: k_stage<4><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    case 6: k_stage<6><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    case 7: k_stage<7><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    case 8: k_stage<8><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    case 9: k_stage<9><<<g, kBlock, 0, c->stream>>>(c->nv, y0, out, s, c->d_ctrl); break;
+    default: sol_set_error("stage with %d terms", k); return SOL_ERR_ARG;
+  }
+  SOL_LAUNCHED();
+  return SOL_OK;
+}
+
+#define RET(x)              \
+  do {                      \
+    int r_ = (x);           \
+    if (r_ != SOL_OK) return r_; \
+  } while (0)
+
+// Force at stage s of the current attempt: time = ctrl->t + c * ctrl->h.
+inline TimeSpec stage_time(sol_ctx* c, double coef) {
+  TimeSpec ts;
+  ts.base = &c->d_ctrl->t;
+  ts.h = &c->d_ctrl->h;
+  ts.c = coef;
+  ts.t_host = 0.0;
+  return ts;
+}
+
+// One RKF78 attempt (RungeKuttaFehlberg78::Step, :147-250): 12 stages, the
+// final sum, the error estimate and its norm.  The time of every stage is the
+// step's start time (:168, :173-234).
+int rkf78_attempt(sol_ctx* c, const double* y0, double* y, double* err) {
+  const Rkf78Stage* st = rkf78_stages();
+  double* fk[13];
+  fk[0] = c->d_accel;
+  for (int k = 1; k < 13; ++k) fk[k] = c->d_fk[k];
+  const uint32_t fl = SOL_EVAL_GAS_DRAG;  // migration only at the Driver's first evaluation (:94-95)
+  for (int r = 1; r <= 12; ++r) {
+    StageArgs s;
+    memset(&s, 0, sizeof(s));
+    for (int k = 0; k < st[r].k; ++k) {
+      s.f[k] = fk[st[r].idx[k]];
+      s.a[k] = st[r].a[k];
+    }
+    RET(launch_stage(c, st[r].k, s, y0, c->d_ytmp));
+    RET(sol_force_launch(c, c->d_ytmp, fk[r], stage_time(c, 0.0), fl));
+  }
+  Rkf78FinalArgs fa;
+  for (int k = 0; k < 13; ++k) fa.f[k] = fk[k];
+  const int g = grid_for(c->nv);
+  k_rkf78_final<<<g, kBlock, 0, c->stream>>>(c->nv, y0, fa, y, err, c->d_yscale, c->d_partial, c->d_ctrl);
+  SOL_LAUNCHED();
+  k_reduce_max<<<1, kBlock, 0, c->stream>>>(c->d_partial, g, c->d_ctrl, 1);
+  SOL_LAUNCHED();
+  return SOL_OK;
+}
+
+int read_ctrl(sol_ctx* c) {
+  SOL_CUDA(cudaMemcpyAsync(c->h_ctrl, c->d_ctrl, sizeof(sol_ctrl), cudaMemcpyDeviceToHost, c->stream));
+  SOL_CUDA(cudaStreamSynchronize(c->stream));
+  return SOL_OK;
+}
+
+int ctrl_status(sol_ctx* c) {
+  int ds = c->h_ctrl->dev_status;
+  if (ds & SOL_DEV_TIMEOUT) {
+    sol_set_error("a bounded device wait ran out");
+    return SOL_ERR_TIMEOUT;
+  }
+  if (ds & SOL_DEV_UNDERFLOW) {
+    sol_set_error("Stepsize-underflow occurred during Runge-Kutta-Fehlberg7(8) step!");
+    return SOL_ERR_UNDERFLOW;
+  }
+  if (ds & SOL_DEV_MAXITER) {
+    sol_set_error("An error occurred during Prince-Dormand driver: iteration number exceeded maxIter!");
+    return SOL_ERR_MAXITER;
+  }
+  return SOL_OK;
+}
+
+int rkf78_driver_step(sol_ctx* c) {
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+  SOL_LAUNCHED();
+  // Driver: all evaluate flags on for the first evaluation (:77-82)
+  RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
+  const int g = grid_for(c->nv);
+  k_yscale<<<g, kBlock, 0, c->stream>>>(c->nv, c->d_y0, c->d_accel, c->d_yscale, c->d_ctrl);
+  SOL_LAUNCHED();
+  for (int attempt = 0;; ++attempt) {
+    RET(rkf78_attempt(c, c->d_y0, c->d_y, c->d_err));
+    k_control_rkf78<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+    SOL_LAUNCHED();
+    RET(read_ctrl(c));
+    RET(ctrl_status(c));
+    if (c->h_ctrl->accepted) break;
+  }
+  SOL_CUDA(cudaMemcpyAsync(c->d_y0, c->d_y, sizeof(double) * c->nv, cudaMemcpyDeviceToDevice, c->stream));
+  return SOL_OK;
+}
+
+int rk4_driver_step(sol_ctx* c) {
+  // RungeKutta4::Driver / Step (RungeKutta4.cpp:20-129)
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+  SOL_LAUNCHED();
+  RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
+  const double a21 = 1.0 / 2.0, a32 = 1.0 / 2.0, a43 = 1.0;
+  const double b1 = 1.0 / 6.0, b2 = 1.0 / 3.0, b3 = 1.0 / 3.0, b4 = 1.0 / 6.0;
+  const double c2 = 1.0 / 2.0, c3 = 1.0 / 2.0, c4 = 1.0;
+  StageArgs s;
+  memset(&s, 0, sizeof(s));
+  s.f[0] = c->d_accel;
+  s.a[0] = a21;
+  RET(launch_stage(c, 1, s, c->d_y0, c->d_ytmp));
+  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[1], stage_time(c, c2), SOL_EVAL_GAS_DRAG));
+  s.f[0] = c->d_fk[1];
+  s.a[0] = a32;
+  RET(launch_stage(c, 1, s, c->d_y0, c->d_ytmp));
+  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[2], stage_time(c, c3), SOL_EVAL_GAS_DRAG));
+  s.f[0] = c->d_fk[2];
+  s.a[0] = a43;
+  RET(launch_stage(c, 1, s, c->d_y0, c->d_ytmp));
+  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[3], stage_time(c, c4), SOL_EVAL_GAS_DRAG));
+  StageArgs fs;
+  memset(&fs, 0, sizeof(fs));
+  fs.f[0] = c->d_accel;
+  fs.f[1] = c->d_fk[1];
+  fs.f[2] = c->d_fk[2];
+  fs.f[3] = c->d_fk[3];
+  fs.a[0] = b1;
+  fs.a[1] = b2;
+  fs.a[2] = b3;
+  fs.a[3] = b4;
+  RET(launch_stage(c, 4, fs, c->d_y0, c->d_y));
+  k_control_rk4<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+  SOL_LAUNCHED();
+  SOL_CUDA(cudaMemcpyAsync(c->d_y0, c->d_y, sizeof(double) * c->nv, cudaMemcpyDeviceToDevice, c->stream));
+  return SOL_OK;
+}
+
+struct DpTab {
+  double b[9], bdh[9], c[9], a[9][8];
+};
+
+const DpTab& dp_tab() {
+  // DormandPrince::DormandPrince (DormandPrince.cpp:37-124)
+  static DpTab T;
+  static bool init = false;
+  if (!init) {
+    memset(&T, 0, sizeof(T));
+    double sQ = sqrt(21.0);
+    T.b[0] = 1.0 / 20.0; T.b[4] = 8.0 / 45.0; T.b[5] = 7.0 * (7.0 + sQ) / 360.0;
+    T.b[6] = 7.0 * (7.0 - sQ) / 360.0; T.b[7] = -1.0 / 20.0; T.b[8] = 1.0 / 20.0;
+    T.bdh[0] = 1.0 / 20.0; T.bdh[4] = 16.0 / 45.0; T.bdh[5] = 49.0 / 180.0; T.bdh[6] = 49.0 / 180.0;
+    T.bdh[7] = 1.0 / 20.0;
+    T.c[1] = 1.0 / 10.0; T.c[2] = 1.0 / 5.0; T.c[3] = 3.0 / 8.0; T.c[4] = 1.0 / 2.0;
+    T.c[5] = (7.0 - sQ) / 14.0; T.c[6] = (7.0 + sQ) / 14.0; T.c[7] = 1.0; T.c[8] = 1.0;
+    T.a[1][0] = 1.0 / 200.0;
+    T.a[2][0] = 1.0 / 150.0; T.a[2][1] = 1.0 / 75.0;
+    T.a[3][0] = 171.0 / 8192.0; T.a[3][1] = 45.0 / 4096.0; T.a[3][2] = 315.0 / 8192.0;
+    T.a[4][0] = 5.0 / 288.0; T.a[4][1] = 25.0 / 528.0; T.a[4][2] = 25.0 / 672.0; T.a[4][3] = 16.0 / 693.0;
+    T.a[5][0] = (1003.0 - 205.0 * sQ) / 12348.0; T.a[5][1] = -25.0 * (751.0 - 173.0 * sQ) / 90552.0;
+    T.a[5][2] = 25.0 * (624.0 - 137.0 * sQ) / 43218.0; T.a[5][3] = -128.0 * (361.0 - 79.0 * sQ) / 237699.0;
+    T.a[5][4] = (3411.0 - 745.0 * sQ) / 24696.0;
+    T.a[6][0] = (793.0 + 187.0 * sQ) / 12348.0; T.a[6][1] = -25.0 * (331.0 + 113.0 * sQ) / 90552.0;
+    T.a[6][2] = 25.0 * (1044.0 + 247.0 * sQ) / 43218.0;
+    T.a[6][3] = -128.0 * (14885.0 + 3779.0 * sQ) / 9745659.0;
+    T.a[6][4] = (3327.0 + 797.0 * sQ) / 24696.0; T.a[6][5] = -(581.0 + 127.0 * sQ) / 1722.0;
+    T.a[7][0] = -(157.0 - 3.0 * sQ) / 378.0; T.a[7][1] = 25.0 * (143.0 - 10.0 * sQ) / 2772.0;
+    T.a[7][2] = -25.0 * (876.0 + 55.0 * sQ) / 3969.0; T.a[7][3] = 1280.0 * (913.0 + 18.0 * sQ) / 596673.0;
+    T.a[7][4] = -(1353.0 + 26.0 * sQ) / 2268.0; T.a[7][5] = 7.0 * (1777.0 + 377.0 * sQ) / 4428.0;
+    T.a[7][6] = 7.0 * (5.0 - sQ) / 36.0;
+    T.a[8][0] = 1.0 / 20.0; T.a[8][4] = 8.0 / 45.0; T.a[8][5] = 7.0 * (7.0 + sQ) / 360.0;
+    T.a[8][6] = 7.0 * (7.0 - sQ) / 360.0;
+    init = true;
+  }
+  return T;
+}
+
+int launch_dp_stage(sol_ctx* c, int k, const DpStageArgs& s) {
+  const int g = grid_for(3 * c->n);
+  switch (k) {
+    case 1: k_dp_stage<1><<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, c->d_ytmp, s, c->d_ctrl); break;
+    case 2: k_dp_stage<2><<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, c->d_ytmp, s, c->d_ctrl); break;
+    case 3: k_dp_stage<3><<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, c->d_ytmp, s, c->d_ctrl); break;
+    case 4: k_dp_stage<4><<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, c->d_ytmp, s, c->d_ctrl); break;
+    case 5: k_dp_stage<5><<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, c->d_ytmp, s, c->d_ctrl); break;
+    case 6: k_dp_stage<6><<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, c->d_ytmp, s, c->d_ctrl); break;
+    case 7: k_dp_stage<7><<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, c->d_ytmp, s, c->d_ctrl); break;
+    default: sol_set_error("dp stage %d", k); return SOL_ERR_ARG;
+  }
+  SOL_LAUNCHED();
+  return SOL_OK;
+}
+
+int dp_driver_step(sol_ctx* c) {
+  const DpTab& T = dp_tab();
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+  SOL_LAUNCHED();
+  RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
+  double* f[9];
+  f[0] = c->d_accel;
+  for (int k = 1; k < 9; ++k) f[k] = c->d_fk[k];
+  for (;;) {
+    for (int k = 1; k < 9; ++k) {
+      DpStageArgs s;
+      memset(&s, 0, sizeof(s));
+      int nt = 0;
+      if (k == 8) {
+        const int idx[4] = {0, 4, 5, 6};
+        for (int q = 0; q < 4; ++q) {
+          s.f[q] = f[idx[q]];
+          s.a[q] = T.a[8][idx[q]];
+        }
+        nt = 4;
+      } else {
+        for (int l = 0; l < k; ++l) {
+          s.f[l] = f[l];
+          s.a[l] = T.a[k][l];
+        }
+        nt = k;
+      }
+      s.ck = T.c[k];
+      RET(launch_dp_stage(c, nt, s));
+      RET(sol_force_launch(c, c->d_ytmp, f[k], stage_time(c, T.c[k]), SOL_EVAL_GAS_DRAG));
+    }
+    DpFinalArgs fa;
+    for (int k = 0; k < 9; ++k) {
+      fa.f[k] = f[k];
+      fa.b[k] = T.b[k];
+      fa.bdh[k] = T.bdh[k];
+    }
+    const int g = grid_for(3 * c->n);
+    k_dp_final<<<g, kBlock, 0, c->stream>>>(c->n, c->d_y0, fa, c->d_y, c->d_err, c->d_partial, c->d_ctrl);
+    SOL_LAUNCHED();
+    k_reduce_max<<<1, kBlock, 0, c->stream>>>(c->d_partial, g, c->d_ctrl, 0);
+    SOL_LAUNCHED();
+    k_control_dp<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+    SOL_LAUNCHED();
+    RET(read_ctrl(c));
+    RET(ctrl_status(c));
+    if (c->h_ctrl->accepted) break;
+  }
+  SOL_CUDA(cudaMemcpyAsync(c->d_y0, c->d_y, sizeof(double) * c->nv, cudaMemcpyDeviceToDevice, c->stream));
+  return SOL_OK;
+}
+
+}  // namespace
+
+int sol_integrator_run(sol_ctx* c, int integrator, int n_steps) {
+  for (int s = 0; s < n_steps; ++s) {
+    int r;
+    if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78) r = rkf78_driver_step(c);
+    else if (integrator == SOL_RUNGE_KUTTA4) r = rk4_driver_step(c);
+    else if (integrator == SOL_DORMAND_PRINCE) r = dp_driver_step(c);
+    else {
+      sol_set_error("unknown integrator %d", integrator);
+      return SOL_ERR_ARG;
+    }
+    if (r != SOL_OK) return r;
+  }
+  return SOL_OK;
+}
+
+int sol_rkf78_single_attempt(sol_ctx* c, double t, double h, const double* d_y0, double* d_y, double* d_err,
+                             double* error_max) {
+  // ctrl t and h from the host, then the Driver's first evaluation, yscale and one attempt
+  sol_ctrl hc;
+  memset(&hc, 0, sizeof(hc));
+  hc.t = t;
+  hc.h = h;
+  hc.h_next = h;
+  hc.eps = c->eps;
+  SOL_CUDA(cudaMemcpyAsync(c->d_ctrl, &hc, sizeof(hc), cudaMemcpyHostToDevice, c->stream));
+  RET(sol_force_launch(c, d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
+  const int g = grid_for(c->nv);
+  k_yscale<<<g, kBlock, 0, c->stream>>>(c->nv, d_y0, c->d_accel, c->d_yscale, c->d_ctrl);
+  SOL_LAUNCHED();
+  RET(rkf78_attempt(c, d_y0, d_y, d_err));
+  RET(read_ctrl(c));
+  RET(ctrl_status(c));
+  *error_max = c->h_ctrl->error_max;
+  return SOL_OK;
+}
+
+int sol_integrate_partials_needed(int nv) { return grid_for(nv); }

@@ -1,0 +1,150 @@
+"""Python handle on one engine context (ctypes over the C-ABI).
+
+:class:`Context` mirrors the reference's C++ surface for the hot path:
+``accel`` is ``Acceleration::Compute`` (Solaris/Acceleration.cpp:60-80),
+``driver`` runs ``RungeKuttaFehlberg78::Driver`` / ``RungeKutta4::Driver`` /
+``DormandPrince::Driver`` calls (Solaris/Simulator.cpp:133-153), ``events``
+evaluates the predicates of ``Simulator::CheckEvent`` and ``integrals`` is
+``Calculate::Integrals``.  Errors raise :class:`abi.SolError` carrying the
+reference-style status code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class Context:
+    def __init__(self, system, device: int = 0, precision: int = abi.PRECISION_FP64, barycentric=None):
+        self.lib = abi.load_library()
+        self.system = system
+        self.n = system.n
+        self._view = abi.BodyDataView(system)
+        self._gas = abi.gas_struct(system.gas) if system.gas is not None else None
+        bary = system.barycentric if barycentric is None else barycentric
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.sol_create(C.byref(self._view.struct),
+                                                C.byref(self._gas) if self._gas is not None else None,
+                                                int(bool(bary)), int(device), C.byref(h)))
+        self.h = h
+        self.set_precision(precision)
+        abi.check(self.lib, self.lib.sol_set_tolerance(self.h, float(system.epsilon)))
+
+    # -- lifetime ---------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sol_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- settings -----------------------------------------------------------------
+    def set_precision(self, precision: int):
+        abi.check(self.lib, self.lib.sol_set_precision(self.h, int(precision)))
+
+    def set_eval_flags(self, flags: int):
+        abi.check(self.lib, self.lib.sol_set_eval_flags(self.h, int(flags)))
+
+    def set_tolerance(self, eps: float):
+        abi.check(self.lib, self.lib.sol_set_tolerance(self.h, float(eps)))
+
+    # -- force ----------------------------------------------------------------
+    def accel(self, t, y, flags=abi.EVAL_ALL):
+        self.set_eval_flags(flags)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        d = np.empty(6 * self.n)
+        rm3, nd = np.empty(self.n), np.empty(self.n)
+        nn = np.empty(self.n, np.int32)
+        abi.check(self.lib, self.lib.sol_accel_compute(self.h, float(t), abi.f64p(y), abi.f64p(d), abi.f64p(rm3),
+                                                       abi.i32p(nn), abi.f64p(nd)))
+        return d, rm3, nn, nd
+
+    def mig_type(self):
+        m = np.empty(self.n, np.int32)
+        abi.check(self.lib, self.lib.sol_get_mig_type(self.h, abi.i32p(m)))
+        return m
+
+    def last_eval(self):
+        rm3, nd = np.empty(self.n), np.empty(self.n)
+        nn = np.empty(self.n, np.int32)
+        abi.check(self.lib, self.lib.sol_get_last_eval(self.h, abi.f64p(rm3), abi.i32p(nn), abi.f64p(nd)))
+        return rm3, nn, nd
+
+    # -- integrators ------------------------------------------------------------
+    def set_state(self, y0):
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        abi.check(self.lib, self.lib.sol_set_state(self.h, abi.f64p(y0)))
+
+    def get_state(self):
+        y = np.empty(6 * self.n)
+        abi.check(self.lib, self.lib.sol_get_state(self.h, abi.f64p(y)))
+        return y
+
+    def driver(self, integrator, t, h, n_steps, time_line=None):
+        tl = time_line or abi.SolTimeLine(float(t), float(h), 0.0)
+        st = abi.SolStepStats()
+        abi.check(self.lib, self.lib.sol_driver(self.h, int(integrator), C.byref(tl), int(n_steps), C.byref(st)))
+        return dict(time=tl.time, h_next=tl.h_next, h_did=tl.h_did,
+                    stats=(st.accepted, st.rejected, st.evaluations), time_line=tl)
+
+    def rkf78_step(self, t, h, y0):
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        y, err, em = np.empty(6 * self.n), np.empty(6 * self.n), np.zeros(1)
+        abi.check(self.lib, self.lib.sol_rkf78_step(self.h, float(t), float(h), abi.f64p(y0), abi.f64p(y),
+                                                    abi.f64p(err), abi.f64p(em)))
+        return y, err, float(em[0])
+
+    # -- measurement ----------------------------------------------------------
+    def stream_handle(self) -> int:
+        v = C.c_void_p()
+        abi.check(self.lib, self.lib.sol_get_stream(self.h, C.byref(v)))
+        return int(v.value or 0)
+
+    def bench_force(self, precision, reps) -> float:
+        ms = C.c_double(0)
+        abi.check(self.lib, self.lib.sol_bench_force(self.h, int(precision), int(reps), C.byref(ms)))
+        return float(ms.value)
+
+    # -- events and integrals ----------------------------------------------------
+    def events(self, ejection, hit_centrum, collision_factor, capacity=4096):
+        ev = (abi.SolEvent * max(capacity, 1))()
+        n = C.c_int32(0)
+        abi.check(self.lib, self.lib.sol_check_events(self.h, float(ejection), float(hit_centrum),
+                                                      float(collision_factor), ev, int(capacity), C.byref(n)))
+        return [(e.kind, e.idx1, e.idx2, e.distance) for e in ev[: min(n.value, capacity)]], n.value
+
+    def integrals(self, y0=None):
+        out = np.zeros(16)
+        yp = None
+        if y0 is not None:
+            y0 = np.ascontiguousarray(y0, dtype=np.float64)
+            yp = abi.f64p(y0)
+        abi.check(self.lib, self.lib.sol_integrals(self.h, yp, abi.f64p(out)))
+        return out
+
+
+def kernel_launches() -> int:
+    lib = abi.load_library()
+    v = C.c_int64(0)
+    lib.sol_kernel_launch_count(C.byref(v))
+    return int(v.value)
+
+
+def fp64_peak_flops(device: int = 0) -> float:
+    lib = abi.load_library()
+    v = C.c_double(0)
+    abi.check(lib, lib.sol_measure_fp64_peak(int(device), C.byref(v)))
+    return float(v.value)

@@ -1,0 +1,149 @@
+"""Integrator drivers on the GPU against fixtures produced by the reference.
+
+With the FP64 force the stage sums, final sums and error estimates follow
+the reference's operation order and are bit-identical per attempt.  The step
+controls call pow(), whose last bit may differ between CUDA and glibc, so
+multi-step trajectories of the adaptive methods are compared to a tolerance;
+RungeKutta4 has no pow and stays bit-identical over many steps."""
+import numpy as np
+import pytest
+
+import oracle
+from solaris_gb300 import abi, engine, scenarios
+
+from golden_io import load, system_from
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
+
+
+def test_rkf78_attempt_bit_exact_config1():
+    d = load("rkf78_step_config1")
+    s = system_from(d)
+    with engine.Context(s) as ctx:
+        y, err, em = ctx.rkf78_step(float(d["meta_t"]), float(d["meta_h"]), s.y0)
+    assert np.array_equal(bits(y), bits(d["out_y"]))
+    assert np.array_equal(bits(err), bits(d["out_error"]))
+    assert np.array_equal(bits([em]), bits(d["out_error_max"]))
+
+
+def test_rkf78_attempt_mixed_gas():
+    """With gas drag the forces carry CUDA-vs-glibc pow/exp rounding (1e-16
+    relative); the error estimate h |f0 + f10 - f11 - f12| 41/840 is a
+    cancellation that amplifies it, so errorMax is compared loosely."""
+    d = load("rkf78_step_mixed_gas")
+    s = system_from(d)
+    with engine.Context(s) as ctx:
+        y, err, em = ctx.rkf78_step(float(d["meta_t"]), float(d["meta_h"]), s.y0)
+    np.testing.assert_allclose(y, d["out_y"], rtol=1e-13, atol=1e-300)
+    ref_em = float(d["out_error_max"][0])
+    assert abs(em - ref_em) <= 1e-3 * ref_em
+
+
+def test_rk4_driver_bit_exact_against_reference():
+    """30 RungeKutta4 driver calls reproduce the reference build bit for bit."""
+    d = load("rk4_driver_selfgrav64")
+    s = system_from(d)
+    n = int(d["meta_nsteps"])
+    with engine.Context(s) as ctx:
+        ctx.set_state(s.y0)
+        tl = abi.SolTimeLine(float(d["meta_t"]), float(d["meta_h"]), 0.0)
+        times = []
+        for _ in range(n):
+            ctx.driver(abi.RUNGE_KUTTA4, 0, 0, 1, time_line=tl)
+            times.append(tl.time)
+        y0 = ctx.get_state()
+        rm3, nn, nd = ctx.last_eval()
+    assert np.array_equal(bits(times), bits(d["out_time"]))
+    assert np.array_equal(bits(y0), bits(d["out_y0"]))
+    assert np.array_equal(nn, d["out_nn_idx"])
+
+
+def _per_step(system, integrator, n_steps, h0, exact):
+    """Each GPU driver call starts from the oracle's state and time line; the
+    oracle is pinned bit-exactly to the reference build (test_oracle_golden)."""
+    o = oracle.Oracle(system)
+    y, t, h = system.y0.copy(), 0.0, h0
+    with engine.Context(system) as ctx:
+        for k in range(n_steps):
+            ro = o.driver(integrator, y, t, h, 1)
+            ctx.set_state(y)
+            tl = abi.SolTimeLine(t, h, 0.0)
+            r = ctx.driver(integrator, 0, 0, 1, time_line=tl)
+            yg = ctx.get_state()
+            assert r["stats"][:2] == ro["stats"][:2], f"step {k}: accepted/rejected differ"
+            if exact:
+                assert np.array_equal(bits(yg), bits(ro["y0"])), f"step {k}"
+                assert tl.time == ro["tl"][0] and tl.h_did == ro["tl"][2]
+                # h_next = 0.9 h errorMax^p: pow() may round differently in the last bit
+                assert abs(tl.h_next - ro["tl"][1]) <= 4e-16 * abs(ro["tl"][1])
+            else:
+                np.testing.assert_allclose(yg, ro["y0"], rtol=1e-12, atol=1e-300)
+                np.testing.assert_allclose(tl.time, ro["tl"][0], rtol=1e-14)
+                np.testing.assert_allclose(tl.h_next, ro["tl"][1], rtol=1e-3)
+            y, t, h = ro["y0"], ro["tl"][0], ro["tl"][1]
+        assert np.array_equal(ctx.mig_type(), o.mig_type())
+
+
+def test_rkf78_driver_per_step_config1():
+    s = scenarios.config1(seed=1501)
+    _per_step(s, abi.RUNGE_KUTTA_FEHLBERG78, 40, s.h0, exact=True)
+
+
+def test_rkf78_driver_per_step_mixed_gas():
+    s = scenarios.mixed_gas_system(seed=3300)
+    _per_step(s, abi.RUNGE_KUTTA_FEHLBERG78, 25, s.h0, exact=False)
+
+
+def test_dormand_prince_driver_per_step_config1():
+    s = scenarios.config1(seed=1502)
+    _per_step(s, abi.DORMAND_PRINCE, 20, s.h0 * 50, exact=True)
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_SPLIT])
+def test_rkf78_long_run_statistics(precision):
+    """500 device-driven RKF78 steps (device-side accept/reject).  Adaptive
+    control is chaotic at the last bit (pow rounding), so the comparison with
+    the oracle is statistical: step counts and reached time agree to a few
+    per cent and both conserve energy to the same order."""
+    s = scenarios.config1(seed=1501)
+    o = oracle.Oracle(s)
+    ref = o.driver(abi.RUNGE_KUTTA_FEHLBERG78, s.y0, 0.0, s.h0, 500)
+    with engine.Context(s, precision=precision) as ctx:
+        e0 = ctx.integrals(s.y0)[15]
+        ctx.set_state(s.y0)
+        r = ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0.0, s.h0, 500)
+        y = ctx.get_state()
+        e1 = ctx.integrals(y)[15]
+    assert r["stats"][0] == 500
+    assert abs(r["stats"][1] - ref["stats"][1]) <= max(3, 0.1 * ref["stats"][1])
+    assert abs(r["time"] - ref["tl"][0]) <= 0.05 * ref["tl"][0]
+    assert abs((e1 - e0) / e0) < 1e-9
+
+
+def test_rk4_full_size_bit_exact_two_steps():
+    """Two RK4 steps of 8,192 self-gravitating bodies: FP64 stays bit-identical
+    to the oracle (no pow in RK4)."""
+    s = scenarios.config3(n=8192)
+    o = oracle.Oracle(s)
+    ref = o.driver(abi.RUNGE_KUTTA4, s.y0, 0.0, s.h0, 2)
+    with engine.Context(s) as ctx:
+        ctx.set_state(s.y0)
+        ctx.driver(abi.RUNGE_KUTTA4, 0.0, s.h0, 2)
+        y = ctx.get_state()
+    assert np.array_equal(bits(y), bits(ref["y0"]))
+
+
+def test_underflow_is_reported():
+    """A tolerance no step can meet shrinks h until t + h == t and the driver
+    returns SOL_ERR_UNDERFLOW (RungeKuttaFehlberg78.cpp:116-122)."""
+    s = scenarios.config3(seed=77, n=17)
+    with engine.Context(s) as ctx:
+        ctx.set_tolerance(1e-300)
+        ctx.set_state(s.y0)
+        with pytest.raises(abi.SolError) as ei:
+            ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 1.0e6, 1.0, 1)
+        assert ei.value.code == abi.SOL_ERR_UNDERFLOW
