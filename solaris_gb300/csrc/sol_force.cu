@@ -13,6 +13,7 @@
 //                 TMA engine) completing on an mbarrier, double buffered.  The
 //                 epilogue adds gas drag and type-I/II migration for the sink.
 #include <cstdio>
+#include <cstring>
 
 #include "sol_internal.cuh"
 
@@ -470,3 +471,4 @@ int sol_force_launch(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts,
 
 int sol_force_tile() { return kTile; }
 int sol_force_prepass_blocks(int npad) { return (npad + kPrepassBlock - 1) / kPrepassBlock; }
+
