@@ -227,6 +227,25 @@ int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double c
 /* ---- diagnostics: Calculate::Integrals (Solaris/Calculate.cpp:43-62). --- */
 int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
 
+/* ---- caller-allocated force evaluation --------------------------------- */
+/* GravityAC alone (no gas terms) for callers that cannot allocate device
+ * memory: a host framework that owns every device byte, a plugin with a fixed
+ * memory budget, or a real-time loop where cudaMalloc would stall.  This entry
+ * point has no counterpart in the reference.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine: all inputs and outputs are device
+ * pointers the caller owns (type[N], mass[N], y[6N] in; dydt[6N], rm3[N],
+ * nn_idx[N], nn_dist[N] out), and its scratch is a fixed array inside the
+ * library (about 1 MiB per device, kept until the process exits), so N is
+ * limited to 16,384 bodies; larger N returns SOL_ERR_ARG.  The first call on
+ * a device resolves that array's device address and should come before any
+ * stream capture.  Work is enqueued on `stream` (a cudaStream_t, NULL for
+ * the default stream) asynchronously.  Every call shares the one array:
+ * calls whose work overlaps on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller. */
+int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_type, const double* d_mass,
+                        const double* d_y, double* d_dydt, double* d_rm3, int32_t* d_nn_idx,
+                        double* d_nn_dist, int32_t precision, void* stream);
+
 /* ---- measurement helpers ------------------------------------------------ */
 /* Measured FP64 fused-multiply-add throughput of this GPU in FLOP/s (FMA = 2). */
 int sol_measure_fp64_peak(int32_t device, double* flops);

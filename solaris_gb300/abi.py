@@ -178,6 +178,8 @@ def _declare(lib):
         "sol_kernel_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
         "sol_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
         "sol_bench_force": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
+        "sol_gravity_noalloc": (C.c_int, [C.POINTER(SolNBodies), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -193,7 +195,7 @@ def exported_names():
         "sol_set_precision", "sol_set_eval_flags", "sol_get_n_total", "sol_accel_compute", "sol_get_mig_type",
         "sol_set_state", "sol_get_state", "sol_set_tolerance", "sol_driver", "sol_driver_host",
         "sol_rkf78_step", "sol_get_last_eval", "sol_check_events", "sol_integrals", "sol_measure_fp64_peak",
-        "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force"]
+        "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc"]
 
 
 def load_library(path: str | None = None):

@@ -14,6 +14,7 @@
 //                 epilogue adds gas drag and type-I/II migration for the sink.
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "sol_internal.cuh"
 
@@ -472,3 +473,127 @@ int sol_force_launch(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts,
 int sol_force_tile() { return kTile; }
 int sol_force_prepass_blocks(int npad) { return (npad + kPrepassBlock - 1) / kPrepassBlock; }
 
+// ---- caller-allocated variant ---------------------------------------------------
+// sol_gravity_noalloc serves callers that must not allocate device memory
+// themselves: code running under someone else's memory manager (a host
+// framework that owns every device byte, a fixed-budget plugin) or in a
+// real-time loop where an allocation would stall.  Its scratch -- the
+// structure-of-arrays source table, the per-block indirect-term partials and
+// a status word -- is this file-scope array, sized for at most
+// kNoAllocMaxBodies bodies (about 1 MiB), present on every device that loads
+// the library until the process exits.
+namespace {
+constexpr int kNoAllocMaxBodies = 16384;
+constexpr int kNoAllocPrepassBlocks = kNoAllocMaxBodies / kPrepassBlock;
+constexpr size_t kNoAllocSrc = (size_t)SRC_ARRAYS * kNoAllocMaxBodies;
+constexpr size_t kNoAllocPart = 6 * (size_t)kNoAllocPrepassBlocks;
+constexpr size_t kNoAllocDoubles = kNoAllocSrc + kNoAllocPart + 8 /* sums */ + 8 /* status */;
+static_assert(kNoAllocMaxBodies % kTile == 0, "scratch must hold whole tiles");
+}  // namespace
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[64];  // device address of g_noalloc_scratch, per device ordinal
+
+// Host code cannot use g_noalloc_scratch as a device address: resolve it once
+// per device, with that device current.
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  SOL_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    sol_set_error("device ordinal %d out of range", dev);
+    return SOL_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return sol_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    g_noalloc_addr[dev] = (double*)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return SOL_OK;
+}
+}  // namespace
+
+extern "C" int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_type, const double* d_mass,
+                                   const double* d_y, double* d_dydt, double* d_rm3, int32_t* d_nn_idx,
+                                   double* d_nn_dist, int32_t precision, void* stream) {
+  if (!counts || !d_type || !d_mass || !d_y || !d_dydt || !d_rm3 || !d_nn_idx || !d_nn_dist) {
+    sol_set_error("sol_gravity_noalloc: null argument");
+    return SOL_ERR_ARG;
+  }
+  const sol_nbodies& k = *counts;
+  const int parts[7] = {k.central_body, k.giant_planet, k.rocky_planet, k.proto_planet, k.super_planetesimal,
+                        k.planetesimal, k.test_particle};
+  long long n = 0;
+  for (int q = 0; q < 7; ++q) {
+    if (parts[q] < 0) {
+      sol_set_error("sol_gravity_noalloc: negative body count");
+      return SOL_ERR_ARG;
+    }
+    n += parts[q];
+  }
+  if (k.central_body != 1) {
+    sol_set_error("sol_gravity_noalloc: need exactly one central body");
+    return SOL_ERR_ARG;
+  }
+  if (n > kNoAllocMaxBodies) {
+    sol_set_error("sol_gravity_noalloc: %lld bodies exceed the fixed scratch capacity of %d bodies", n,
+                  kNoAllocMaxBodies);
+    return SOL_ERR_ARG;
+  }
+  if (precision != SOL_PRECISION_FP64 && precision != SOL_PRECISION_SPLIT) {
+    sol_set_error("sol_gravity_noalloc: unknown precision %d", precision);
+    return SOL_ERR_ARG;
+  }
+  double* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != SOL_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  ForceCtx fc;
+  memset(&fc, 0, sizeof(fc));
+  fc.cls.n = (int)n;
+  fc.cls.n_central = k.central_body;
+  fc.cls.n_giant = k.giant_planet;
+  fc.cls.n_rocky = k.rocky_planet;
+  fc.cls.n_proto = k.proto_planet;
+  fc.cls.n_spl = k.super_planetesimal;
+  fc.cls.n_pl = k.planetesimal;
+  fc.cls.nm = k.central_body + k.giant_planet + k.rocky_planet + k.proto_planet;
+  fc.npad = (int)(((n + kTile - 1) / kTile) * kTile);
+  fc.precision = precision;
+  fc.type = d_type;
+  fc.mass = d_mass;
+  fc.rm3 = d_rm3;
+  fc.nn_idx = d_nn_idx;
+  fc.nn_dist = d_nn_dist;
+  fc.src = scratch;  // SRC_ARRAYS x npad doubles at stride npad
+  fc.ind_part = scratch + kNoAllocSrc;
+  fc.ind_sum = scratch + kNoAllocSrc + kNoAllocPart;
+  fc.n_ind_blocks = (fc.npad + kPrepassBlock - 1) / kPrepassBlock;
+  int* status = (int*)(scratch + kNoAllocSrc + kNoAllocPart + 8);
+  // The array keeps the previous call's contents: the source table and the
+  // partials are rewritten in full below, the status word must start at zero.
+  SOL_CUDA(cudaMemsetAsync(status, 0, sizeof(int), st));
+  // rm3[0] (the central body) is never computed and reads as 0, as in the
+  // reference, whose rm3 array starts zeroed (Acceleration.cpp:65-69).
+  SOL_CUDA(cudaMemsetAsync(d_rm3, 0, sizeof(double), st));
+  const int split = precision == SOL_PRECISION_SPLIT;
+  k_prepass<<<fc.n_ind_blocks, kPrepassBlock, 0, st>>>(fc, d_y, split);
+  SOL_LAUNCHED();
+  if (split) {
+    k_ind_reduce<<<1, 256, 0, st>>>(fc);
+    SOL_LAUNCHED();
+  }
+  TimeSpec ts{nullptr, nullptr, 0.0, 0.0};
+  const int nb = (int)((n + kSinkBlock - 1) / kSinkBlock);
+  if (split)
+    k_gravity_ac<SOL_PRECISION_SPLIT><<<nb, kSinkBlock, 0, st>>>(fc, d_y, d_dydt, ts, 0u, status);
+  else
+    k_gravity_ac<SOL_PRECISION_FP64><<<nb, kSinkBlock, 0, st>>>(fc, d_y, d_dydt, ts, 0u, status);
+  SOL_LAUNCHED();
+  return SOL_OK;
+}
