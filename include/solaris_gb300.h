@@ -71,8 +71,14 @@ enum sol_integrator_type {
  *  SPLIT: FP64 displacement and r^2; 1/r^3 from an FP32 rsqrt seed plus one
  *         FP64 Newton correction (carried to second order in the residual);
  *         per-tile partial sums folded with compensated two-sum.  Relative
- *         acceleration error against FP64 well below 1e-12.               */
-enum sol_precision { SOL_PRECISION_FP64 = 0, SOL_PRECISION_SPLIT = 1 };
+ *         acceleration error against FP64 well below 1e-12.
+ *  SPLIT_FF: the displacement stays FP64 (3 FP64 instructions per pair); r^2,
+ *         the FP32 rsqrt seed with its Newton correction, G m r^-3 and the
+ *         accumulation run in float-float (pairs of FP32 numbers, ~48-bit
+ *         significand) on the FP32 pipe; tile sums are folded into FP64.
+ *         Same 1e-12 relative bound; requires pair distances above 1e-12 AU
+ *         for the float-float branch (closer pairs fall back to FP64).       */
+enum sol_precision { SOL_PRECISION_FP64 = 0, SOL_PRECISION_SPLIT = 1, SOL_PRECISION_SPLIT_FF = 2 };
 
 /* Acceleration::evaluate* switches (Solaris/Acceleration.h:375-377) */
 #define SOL_EVAL_GAS_DRAG 1u
@@ -207,6 +213,11 @@ int sol_get_mig_type(const sol_ctx* ctx, int32_t* mig_type);
 int sol_set_state(sol_ctx* ctx, const double* y0);   /* host y0[6N] -> device */
 int sol_get_state(sol_ctx* ctx, double* y0);         /* device -> host y0[6N] */
 int sol_set_tolerance(sol_ctx* ctx, double epsilon); /* RKF78/DP epsilon (1e-10 by default) */
+/* RKF78 / DP driver calls run as one CUDA graph each, whose attempt loop is a
+ * device-side conditional WHILE node (default, enable = 1), or with the host
+ * reading the control block after every attempt (enable = 0).  Results are
+ * identical. */
+int sol_set_device_loop(sol_ctx* ctx, int32_t enable);
 int sol_driver(sol_ctx* ctx, int32_t integrator, sol_time_line* tl, int32_t n_steps,
                sol_step_stats* stats);
 /* Convenience: host y0 in, host y0 out around sol_driver. */

@@ -36,7 +36,7 @@ GAS_CONSTANT, GAS_LINEAR, GAS_EXPONENTIAL = 0, 1, 2
 # IntegratorType (Solaris/IntegratorType.h)
 DORMAND_PRINCE, RUNGE_KUTTA4, RUNGE_KUTTA56, RUNGE_KUTTA_FEHLBERG78 = 0, 1, 2, 3
 # sol_precision
-PRECISION_FP64, PRECISION_SPLIT = 0, 1
+PRECISION_FP64, PRECISION_SPLIT, PRECISION_SPLIT_FF = 0, 1, 2
 # evaluate flags
 EVAL_GAS_DRAG, EVAL_TYPE_I, EVAL_TYPE_II, EVAL_ALL = 1, 2, 4, 7
 # quirks
@@ -166,6 +166,7 @@ def _declare(lib):
         "sol_set_state": (C.c_int, [P, _PF64]),
         "sol_get_state": (C.c_int, [P, _PF64]),
         "sol_set_tolerance": (C.c_int, [P, C.c_double]),
+        "sol_set_device_loop": (C.c_int, [P, C.c_int32]),
         "sol_driver": (C.c_int, [P, C.c_int32, C.POINTER(SolTimeLine), C.c_int32, C.POINTER(SolStepStats)]),
         "sol_driver_host": (C.c_int, [P, C.c_int32, _PF64, C.POINTER(SolTimeLine), C.c_int32,
                                       C.POINTER(SolStepStats)]),
@@ -193,7 +194,7 @@ def exported_names():
     return [
         "sol_last_error", "sol_version", "sol_gas_component_init", "sol_create", "sol_destroy",
         "sol_set_precision", "sol_set_eval_flags", "sol_get_n_total", "sol_accel_compute", "sol_get_mig_type",
-        "sol_set_state", "sol_get_state", "sol_set_tolerance", "sol_driver", "sol_driver_host",
+        "sol_set_state", "sol_get_state", "sol_set_tolerance", "sol_set_device_loop", "sol_driver", "sol_driver_host",
         "sol_rkf78_step", "sol_get_last_eval", "sol_check_events", "sol_integrals", "sol_measure_fp64_peak",
         "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc"]
 

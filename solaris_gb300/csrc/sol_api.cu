@@ -11,6 +11,7 @@
 #include "sol_internal.cuh"
 
 int sol_force_tile();
+int sol_force_part_doubles(int npad);
 int sol_force_prepass_blocks(int npad);
 int sol_integrate_partials_needed(int nv);
 int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_pe);
@@ -18,6 +19,8 @@ int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_pe);
 // ---- errors and counters -----------------------------------------------------
 static thread_local char g_err[1024] = "";
 static std::atomic<long long> g_launches{0};
+static thread_local int g_capturing = 0;
+static thread_local long long g_captured = 0;
 
 void sol_set_error(const char* fmt, ...) {
   va_list ap;
@@ -31,7 +34,20 @@ int sol_cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
   return SOL_ERR_CUDA;
 }
 
-void sol_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// Kernels launched into a stream capture are counted per captured kernel and
+// added to the launch count each time their graph runs.
+void sol_count_launch() {
+  if (g_capturing)
+    ++g_captured;
+  else
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void sol_capture_begin() {
+  g_capturing = 1;
+  g_captured = 0;
+}
+void sol_capture_end() { g_capturing = 0; }
+long long sol_capture_count() { return g_captured; }
 
 #define RET(x)                   \
   do {                           \
@@ -121,11 +137,12 @@ void free_ctx(sol_ctx* c) {
   void* ptrs[] = {c->d_type, c->d_mig_type, c->d_mig_stop_at, c->d_mass, c->d_radius, c->d_density, c->d_cd,
                   c->d_gs, c->d_ge, c->d_rm3, c->d_nn_dist, c->d_src, c->d_drag, c->d_mig1, c->d_mig2,
                   c->d_ind_part, c->d_ind_sum, c->d_nn_idx, c->d_y0, c->d_y, c->d_accel, c->d_yscale, c->d_err,
-                  c->d_ytmp, c->d_io_in, c->d_io_out, c->d_partial, c->d_ctrl};
+                  c->d_ytmp, c->d_io_in, c->d_io_out, c->d_partial, c->d_ctrl, c->d_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < 13; ++k)
     if (c->d_fk[k]) cudaFree(c->d_fk[k]);
+  for (int k = 0; k < 2; ++k) sol_graph_release(c->graphs[k]);
   if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -247,6 +264,7 @@ int sol_create(const sol_body_data* b, const sol_gas_component* gas, int32_t bar
   c->precision = SOL_PRECISION_FP64;
   c->eval_flags = SOL_EVAL_ALL;
   c->eps = pow(10, -10.0);  // RungeKuttaFehlberg78.cpp:38-39
+  c->device_loop = 1;
   c->has_gas = gas != nullptr;
   if (gas) c->gas_host = *gas;
   Classes& cl = c->cls;
@@ -286,7 +304,9 @@ int sol_create(const sol_body_data* b, const sol_gas_component* gas, int32_t bar
   for (int q = 0; q < 13; ++q)
     if ((rc = dev_alloc(&c->d_fk[q], NV))) return fail(rc);
   c->n_partial = sol_integrate_partials_needed(NV);
-  if ((rc = dev_alloc(&c->d_partial, (size_t)c->n_partial + 16)) || (rc = dev_alloc(&c->d_ctrl, 1))) return fail(rc);
+  if ((rc = dev_alloc(&c->d_partial, (size_t)c->n_partial + 16)) || (rc = dev_alloc(&c->d_ctrl, 1)) ||
+      (rc = dev_alloc(&c->d_part, (size_t)sol_force_part_doubles(c->npad))))
+    return fail(rc);
   if (cudaMallocHost((void**)&c->h_ctrl, sizeof(sol_ctrl)) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_stage, sizeof(double) * NV) != cudaSuccess) {
     sol_set_error("cudaMallocHost failed");
@@ -351,7 +371,7 @@ int sol_destroy(sol_ctx* c) {
 
 int sol_set_precision(sol_ctx* c, int32_t p) {
   RET(check_ctx(c));
-  if (p != SOL_PRECISION_FP64 && p != SOL_PRECISION_SPLIT) {
+  if (p != SOL_PRECISION_FP64 && p != SOL_PRECISION_SPLIT && p != SOL_PRECISION_SPLIT_FF) {
     sol_set_error("unknown precision %d", p);
     return SOL_ERR_ARG;
   }
@@ -429,6 +449,12 @@ int sol_get_state(sol_ctx* c, double* y0) {
   return SOL_OK;
 }
 
+int sol_set_device_loop(sol_ctx* c, int32_t enable) {
+  RET(check_ctx(c));
+  c->device_loop = enable ? 1 : 0;
+  return SOL_OK;
+}
+
 int sol_set_tolerance(sol_ctx* c, double eps) {
   RET(check_ctx(c));
   if (!(eps > 0)) {
@@ -458,10 +484,32 @@ int sol_driver(sol_ctx* c, int32_t integrator, sol_time_line* tl, int32_t n_step
   h0.h = tl->h_next;
   h0.eps = c->eps;
   SOL_CUDA(cudaMemcpyAsync(c->d_ctrl, &h0, sizeof(h0), cudaMemcpyHostToDevice, c->stream));
+  c->graph_steps = 0;
+  c->graph_used = 0;
   int rc = sol_integrator_run(c, integrator, n_steps);
   SOL_CUDA(cudaMemcpyAsync(c->h_ctrl, c->d_ctrl, sizeof(sol_ctrl), cudaMemcpyDeviceToHost, c->stream));
   SOL_CUDA(cudaStreamSynchronize(c->stream));
   const sol_ctrl& hc = *c->h_ctrl;
+  if (c->graph_used) {
+    const DriverGraph& G = c->graphs[c->graph_used - 1];
+    const long long attempts = hc.n_accepted + hc.n_rejected;
+    g_launches.fetch_add(c->graph_steps * (G.k_pro + G.k_epi) + attempts * G.k_body, std::memory_order_relaxed);
+  }
+  if (rc == SOL_OK) rc = [&]() {
+    if (hc.dev_status & SOL_DEV_TIMEOUT) {
+      sol_set_error("a bounded device wait ran out");
+      return (int)SOL_ERR_TIMEOUT;
+    }
+    if (hc.dev_status & SOL_DEV_UNDERFLOW) {
+      sol_set_error("Stepsize-underflow occurred during Runge-Kutta-Fehlberg7(8) step!");
+      return (int)SOL_ERR_UNDERFLOW;
+    }
+    if (hc.dev_status & SOL_DEV_MAXITER) {
+      sol_set_error("An error occurred during Prince-Dormand driver: iteration number exceeded maxIter!");
+      return (int)SOL_ERR_MAXITER;
+    }
+    return (int)SOL_OK;
+  }();
   tl->time = hc.t;
   tl->h_next = hc.h_next;
   tl->h_did = hc.h_did;

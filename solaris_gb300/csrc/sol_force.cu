@@ -24,7 +24,11 @@ constexpr int kSinkBlock = 128;  // sinks per CTA
 constexpr int kTile = 256;       // sources per shared-memory tile
 constexpr int kPrepassBlock = 256;
 
-enum SrcArray { SX = 0, SY, SZ, SGM, SPX, SPY, SPZ, SRC_ARRAYS = 8 };
+enum SrcArray { SX = 0, SY, SZ, SGM, SPX, SPY, SPZ, SGF, SRC_ARRAYS = 8 };  // SGF: G m as (hi, lo) floats
+
+constexpr int kChunkTiles = 16;             // sources per work unit of the 2-D pair kernel
+constexpr int kChunk = kChunkTiles * kTile;  // 4,096
+enum PartSlot { PAX = 0, PAY, PAZ, PR2, PIDX, PART_SLOTS = 5 };
 
 __device__ __forceinline__ double eval_time(const TimeSpec& ts) {
   return ts.base ? (*ts.base + ts.c * (*ts.h)) : ts.t_host;
@@ -74,6 +78,9 @@ __global__ void k_prepass(ForceCtx fc, const double* __restrict__ y, int split) 
     s[SPX * np + j] = px;
     s[SPY * np + j] = py;
     s[SPZ * np + j] = pz;
+    float gh = __double2float_rn(gm);
+    float gl = __double2float_rn(gm - (double)gh);
+    reinterpret_cast<float2*>(s + (size_t)SGF * np)[j] = make_float2(gh, gl);
   }
   if (!split) return;
   // fixed-order block tree reduction of the indirect contributions
@@ -300,16 +307,17 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
     const uint32_t parity = (t >> 1) & 1;
     const bool ok = sol_mbar_wait(&sm.bar[st], parity);
     const int j0 = t * kTile;
+    const int jmax = min(kTile, ns_cta - j0);  // sources beyond the CTA's range are never read
     if (ok && i < n && i >= 1) {
       if constexpr (PREC == SOL_PRECISION_FP64) {
 #pragma unroll 4
-        for (int jj = 0; jj < kTile; ++jj)
+        for (int jj = 0; jj < jmax; ++jj)
           pair_fp64(*reinterpret_cast<TileSmem<7>*>(&sm), st, jj, j0 + jj, i, ns, xi, yi, zi, ax, ay, az, rminb,
                     nn);
       } else {
         double tx = 0.0, ty = 0.0, tz = 0.0;
 #pragma unroll 4
-        for (int jj = 0; jj < kTile; ++jj)
+        for (int jj = 0; jj < jmax; ++jj)
           pair_split(*reinterpret_cast<TileSmem<4>*>(&sm), st, jj, j0 + jj, i, ns, xi, yi, zi, tx, ty, tz, rminb,
                      nn);
         two_sum(sx, cx, tx);
@@ -373,8 +381,15 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
     a[0] += (sx + cx) - (S[0] - own[0]);
     a[1] += (sy + cy) - (S[1] - own[1]);
     a[2] += (sz + cz) - (S[2] - own[2]);
+    // the reference's rij for the chosen neighbour (Acceleration.cpp:301-305), bit for bit
+    double rij = 0.0;
+    if (nn >= 0) {
+      const double xij = y[6 * nn + 0] - xi, yij = y[6 * nn + 1] - yi, zij = y[6 * nn + 2] - zi;
+      rij = __dsqrt_rn(xij * xij + yij * yij + zij * zij);
+      if (!(rij < 1.0e10)) nn = -1;
+    }
     fc.nn_idx[i] = nn;
-    fc.nn_dist[i] = nn >= 0 ? __dsqrt_rn(__longlong_as_double(rminb)) : 0.0;
+    fc.nn_dist[i] = nn >= 0 ? rij : 0.0;
   }
   add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
   out[0] = yv[3];
@@ -433,12 +448,314 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_bc(ForceCtx fc, const do
   out[5] = a[2];
 }
 
+
+// ---- float-float arithmetic (pairs of FP32 numbers, ~48-bit significand) ------
+// Error-free transformations (Knuth's TwoSum, Dekker's FastTwoSum, TwoProduct
+// by FMA); the library is built with --fmad=false, so no other contraction
+// disturbs them.
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void ff_fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+  s = a + b;
+  e = b - (s - a);
+}
+__device__ __forceinline__ void ff_two_prod(float a, float b, float& p, float& e) {
+  p = a * b;
+  e = __fmaf_rn(a, b, -p);
+}
+
+// FP64 -> (hi, lo) floats by integer operations on the bit pattern (no F2F,
+// which would occupy the FP64 pipe): hi keeps the leading 24 significant bits
+// (truncated), lo the next 24 of the remaining 29 (rounded by I2F).
+// |d| outside [2^-126, 2^128) maps to (0, 0); displacements between distinct
+// bodies are far inside that range.
+__device__ __forceinline__ void ff_from_double(double d, float& h, float& l) {
+  const unsigned hi = (unsigned)__double2hiint(d);
+  const unsigned lo = (unsigned)__double2loint(d);
+  const int e = (int)((hi >> 20) & 0x7FFu);
+  const unsigned sign = hi & 0x80000000u;
+  const bool in_range = (e >= 897) & (e <= 1150);
+  const unsigned hbits = sign | ((unsigned)(e - 896) << 23) | ((hi & 0x000FFFFFu) << 3) | (lo >> 29);
+  h = in_range ? __uint_as_float(hbits) : 0.0f;
+  const int es = e - 1023 - 52 + 127;  // biased exponent of 2^(E-52)
+  const float scale = (es >= 1 && in_range) ? __uint_as_float((unsigned)es << 23) : 0.0f;
+  const float m = __uint2float_rn(lo & 0x1FFFFFFFu) * scale;
+  l = __uint_as_float(__float_as_uint(m) | sign);
+}
+
+// Float-float pair: FP64 displacement (3 DADD, the only FP64 instructions),
+// r^2 with exact squares and sums, FP32 rsqrt seed and one Newton correction
+// r^-3 = y^3 (1 + 3/2 e + 15/8 e^2) with e = 1 - r^2 y^2 evaluated from exact
+// products, G m r^-3 d and the accumulation in float-float.  Pairs closer
+// than 1e-12 AU (where r^-3 would leave the FP32 range) take the FP64 split
+// arithmetic instead.
+struct FFAcc {
+  float h[3], l[3];
+};
+
+__device__ __forceinline__ void pair_ff(const double* __restrict__ sx, const double* __restrict__ sy,
+                                        const double* __restrict__ sz, const float2* __restrict__ sg, int jj, int j,
+                                        int i, int ns, double xi, double yi, double zi, FFAcc& A, double& fbx,
+                                        double& fby, double& fbz, float& mh, float& ml, int& nn) {
+  const double dxd = sx[jj] - xi, dyd = sy[jj] - yi, dzd = sz[jj] - zi;
+  float dh[3], dl[3];
+  ff_from_double(dxd, dh[0], dl[0]);
+  ff_from_double(dyd, dh[1], dl[1]);
+  ff_from_double(dzd, dh[2], dl[2]);
+  float p1, e1, p2, e2, p3, e3;
+  ff_two_prod(dh[0], dh[0], p1, e1);
+  ff_two_prod(dh[1], dh[1], p2, e2);
+  ff_two_prod(dh[2], dh[2], p3, e3);
+  float s12, t12, s3, t3;
+  ff_two_sum(p1, p2, s12, t12);
+  ff_two_sum(s12, p3, s3, t3);
+  float lo = ((t12 + t3) + (e1 + e2)) + e3;
+  lo = __fmaf_rn(dh[0] + dh[0], dl[0], lo);
+  lo = __fmaf_rn(dh[1] + dh[1], dl[1], lo);
+  lo = __fmaf_rn(dh[2] + dh[2], dl[2], lo);
+  float r2h, r2l;
+  ff_fast_two_sum(s3, lo, r2h, r2l);
+  const float2 g = (j < ns) ? sg[jj] : make_float2(0.0f, 0.0f);  // G m of j = 0 and padding is 0
+  if (r2h < 1.0e-24f && r2h > 0.0f) {  // extremely close pair: FP64 split arithmetic
+    double r2 = __fma_rn(dxd, dxd, __fma_rn(dyd, dyd, dzd * dzd));
+    double rinv = __drcp_rn(__dsqrt_rn(r2));
+    double sd = ((double)g.x + (double)g.y) * (rinv * rinv * rinv);
+    fbx = __fma_rn(sd, dxd, fbx);
+    fby = __fma_rn(sd, dyd, fby);
+    fbz = __fma_rn(sd, dzd, fbz);
+  } else {
+    const float y = rsqrtf(fmaxf(r2h, 1.0e-24f));  // the sink itself: r2 = 0, contribution 0 * d = 0
+    float y2, y2e, q, qe;
+    ff_two_prod(y, y, y2, y2e);
+    ff_two_prod(r2h, y2, q, qe);
+    const float e = ((1.0f - q) - qe) - __fmaf_rn(r2h, y2e, r2l * y2);
+    float y3h, y3e;
+    ff_two_prod(y2, y, y3h, y3e);
+    y3e = __fmaf_rn(y2e, y, y3e);
+    const float c = e * __fmaf_rn(1.875f, e, 1.5f);
+    float Rh, Rl;
+    ff_fast_two_sum(y3h, __fmaf_rn(y3h, c, y3e), Rh, Rl);
+    float sh, se;
+    ff_two_prod(g.x, Rh, sh, se);
+    se = __fmaf_rn(g.x, Rl, __fmaf_rn(g.y, Rh, se));
+    ff_fast_two_sum(sh, se, sh, se);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float ah, ae;
+      ff_two_prod(sh, dh[k], ah, ae);
+      ae = __fmaf_rn(sh, dl[k], __fmaf_rn(se, dh[k], ae));
+      float s1, s2;
+      ff_two_sum(A.h[k], ah, s1, s2);
+      s2 = s2 + (A.l[k] + ae);
+      ff_fast_two_sum(s1, s2, A.h[k], A.l[k]);
+    }
+  }
+  const bool better = ((r2h < mh) | ((r2h == mh) & (r2l < ml))) & (j >= 1) & (j < ns) & (j != i);
+  mh = better ? r2h : mh;
+  ml = better ? r2l : ml;
+  nn = better ? j : nn;
+}
+
+// 2-D pair kernel of the split forms: blockIdx.x = block of kSinkBlock sinks,
+// blockIdx.y = chunk of kChunk sources.  Each CTA writes, per sink, its
+// partial acceleration sum and nearest-neighbour candidate for the chunk;
+// k_combine adds the chunks in a fixed order.  Many small work units let the
+// block scheduler balance the FP64 pipe load across SMs.
+template <int MODE>
+__global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double* __restrict__ y,
+                                                      double* __restrict__ part, int* dev_status) {
+  constexpr int NARR = 4;  // x, y, z and G m (FP64 for SPLIT, float-float for SPLIT_FF)
+  __shared__ __align__(128) TileSmem<NARR> sm;
+  const Classes& c = fc.cls;
+  const int n = c.n;
+  const int np = fc.npad;
+  const int i = blockIdx.x * kSinkBlock + threadIdx.x;
+  const int i_first = blockIdx.x * kSinkBlock;
+  const int ns_cta = (fc.type[min(i_first, n - 1)] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
+  const int ns = (i < n && fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
+  const int j_begin = blockIdx.y * kChunk;
+  const int j_end = min(j_begin + kChunk, ns_cta);
+  const int t_begin = j_begin / kTile;
+  const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
+  const int arr[NARR] = {SX, SY, SZ, MODE == SOL_PRECISION_SPLIT ? SGM : SGF};
+
+  double xi = 0, yi = 0, zi = 0;
+  if (i < n) {
+    xi = y[6 * i + 0];
+    yi = y[6 * i + 1];
+    zi = y[6 * i + 2];
+  }
+  if (threadIdx.x == 0) {
+    sol_mbar_init(&sm.bar[0], 1);
+    sol_mbar_init(&sm.bar[1], 1);
+    sol_fence_barrier_init();
+  }
+  __syncthreads();
+  auto issue = [&](int t, int stage) {
+    sol_mbar_expect_tx(&sm.bar[stage], NARR * kTile * 8);
+    for (int k = 0; k < NARR; ++k)
+      sol_bulk_g2s(&sm.v[stage][k][0], fc.src + (size_t)arr[k] * np + (size_t)(t_begin + t) * kTile, kTile * 8,
+                   &sm.bar[stage]);
+  };
+  if (threadIdx.x == 0) {
+    if (ntiles > 0) issue(0, 0);
+    if (ntiles > 1) issue(1, 1);
+  }
+  double ax = 0.0, ay = 0.0, az = 0.0;  // chunk sums of the per-tile partials
+  double cx = 0.0, cy = 0.0, cz = 0.0;  // compensation terms
+  long long r2minb = __double_as_longlong(1.0e20);
+  float mh = 1.0e20f, ml = 0.0f;
+  int nn = -1;
+  int issued = ntiles < 2 ? ntiles : 2;
+  int t = 0;
+  bool timed_out = false;
+  for (; t < ntiles; ++t) {
+    const int st = t & 1;
+    const bool ok = sol_mbar_wait(&sm.bar[st], (t >> 1) & 1);
+    const int j0 = (t_begin + t) * kTile;
+    const int jmax = min(kTile, j_end - j0);  // sources beyond the chunk's range are never read
+    if (ok && i < n && i >= 1) {
+      if constexpr (MODE == SOL_PRECISION_SPLIT) {
+        double tx = 0.0, ty = 0.0, tz = 0.0;
+#pragma unroll 4
+        for (int jj = 0; jj < jmax; ++jj)
+          pair_split(*reinterpret_cast<TileSmem<4>*>(&sm), st, jj, j0 + jj, i, ns, xi, yi, zi, tx, ty, tz, r2minb,
+                     nn);
+        two_sum(ax, cx, tx);
+        two_sum(ay, cy, ty);
+        two_sum(az, cz, tz);
+      } else {
+        FFAcc A;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) A.h[k] = A.l[k] = 0.0f;
+        double fbx = 0.0, fby = 0.0, fbz = 0.0;
+        const float2* sg = reinterpret_cast<const float2*>(&sm.v[st][3][0]);
+#pragma unroll 2
+        for (int jj = 0; jj < jmax; ++jj)
+          pair_ff(&sm.v[st][0][0], &sm.v[st][1][0], &sm.v[st][2][0], sg, jj, j0 + jj, i, ns, xi, yi, zi, A, fbx, fby,
+                  fbz, mh, ml, nn);
+        // fold the tile's float-float partial into the FP64 chunk sums
+        two_sum(ax, cx, ((double)A.h[0] + (double)A.l[0]) + fbx);
+        two_sum(ay, cy, ((double)A.h[1] + (double)A.l[1]) + fby);
+        two_sum(az, cz, ((double)A.h[2] + (double)A.l[2]) + fbz);
+      }
+    }
+    if (__syncthreads_or(!ok)) {
+      timed_out = true;
+      break;
+    }
+    if (threadIdx.x == 0 && t + 2 < ntiles) {
+      sol_fence_proxy_async();
+      issue(t + 2, st);
+    }
+    if (t + 2 < ntiles) issued = t + 3;
+  }
+  if (timed_out) {
+    if (threadIdx.x == 0) {
+      atomicOr(dev_status, SOL_DEV_TIMEOUT);
+      for (int u = t; u < issued; ++u) sol_mbar_wait(&sm.bar[u & 1], (u >> 1) & 1);
+    }
+    __syncthreads();
+    return;
+  }
+  if (i >= n) return;
+  const size_t base = (size_t)blockIdx.y * PART_SLOTS * np + i;
+  part[base + PAX * np] = ax + cx;
+  part[base + PAY * np] = ay + cy;
+  part[base + PAZ * np] = az + cz;
+  const double r2min =
+      (MODE == SOL_PRECISION_SPLIT) ? __longlong_as_double(r2minb) : (double)mh + (double)ml;
+  part[base + PR2 * np] = nn >= 0 ? r2min : 1.0e300;
+  part[base + PIDX * np] = __longlong_as_double((long long)nn);
+}
+
+// Per sink: the chunk partials in chunk order, the nearest neighbour (the
+// smallest r^2, ties to the lower index as the reference's ascending scan),
+// distanceOfNN recomputed in the reference's FP64 arithmetic for the chosen
+// neighbour, the Kepler and indirect terms, and the gas terms.
+__global__ void k_combine(ForceCtx fc, const double* __restrict__ y, double* __restrict__ dydt,
+                          const double* __restrict__ part, int nchunk, TimeSpec ts, uint32_t flags) {
+  const Classes& c = fc.cls;
+  const int n = c.n;
+  const int np = fc.npad;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double* out = dydt + 6 * i;
+  if (i == 0) {
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    fc.nn_idx[0] = -1;
+    fc.nn_dist[0] = 0.0;
+    return;
+  }
+  const double* yv = y + 6 * i;
+  double sx = 0.0, sy = 0.0, sz = 0.0, ex = 0.0, ey = 0.0, ez = 0.0;
+  double best = 1.0e300;
+  int nn = -1;
+  for (int ch = 0; ch < nchunk; ++ch) {
+    const size_t base = (size_t)ch * PART_SLOTS * np + i;
+    two_sum(sx, ex, part[base + PAX * np]);
+    two_sum(sy, ey, part[base + PAY * np]);
+    two_sum(sz, ez, part[base + PAZ * np]);
+    const double r2 = part[base + PR2 * np];
+    const int j = (int)__double_as_longlong(part[base + PIDX * np]);
+    if (j >= 0 && r2 < best) {
+      best = r2;
+      nn = j;
+    }
+  }
+  const int ns = (fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
+  const double mu = SOL_GAUSS2 * (fc.mass[0] + fc.mass[i]);
+  const double rm3i = fc.rm3[i];
+  const double xi = yv[0], yi = yv[1], zi = yv[2];
+  double a[3];
+  a[0] = -mu * rm3i * xi;
+  a[1] = -mu * rm3i * yi;
+  a[2] = -mu * rm3i * zi;
+  const double* S = fc.ind_sum + ((fc.type[i] <= SOL_PROTO_PLANET) ? 3 : 0);
+  const double* s = fc.src;
+  double own[3] = {0.0, 0.0, 0.0};
+  if (i < ns) {
+    const double gmi = s[SGM * np + i];
+    own[0] = gmi * s[SPX * np + i];
+    own[1] = gmi * s[SPY * np + i];
+    own[2] = gmi * s[SPZ * np + i];
+  }
+  a[0] += (sx + ex) - (S[0] - own[0]);
+  a[1] += (sy + ey) - (S[1] - own[1]);
+  a[2] += (sz + ez) - (S[2] - own[2]);
+  if (nn >= 0) {
+    // the reference's rij for this j (Acceleration.cpp:301-305), bit for bit
+    const double xij = y[6 * nn + 0] - xi, yij = y[6 * nn + 1] - yi, zij = y[6 * nn + 2] - zi;
+    const double rij = __dsqrt_rn(xij * xij + yij * yij + zij * zij);
+    if (rij < 1.0e10) {
+      fc.nn_idx[i] = nn;
+      fc.nn_dist[i] = rij;
+    } else {
+      fc.nn_idx[i] = -1;
+      fc.nn_dist[i] = 0.0;
+    }
+  } else {
+    fc.nn_idx[i] = -1;
+    fc.nn_dist[i] = 0.0;
+  }
+  add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
+  out[0] = yv[3];
+  out[1] = yv[4];
+  out[2] = yv[5];
+  out[3] = a[0];
+  out[4] = a[1];
+  out[5] = a[2];
+}
+
 }  // namespace
 
 // parts: 1 = prepass (and indirect totals), 2 = pair kernel, 3 = both.
 int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int parts) {
   ForceCtx& fc = c->fc;
-  const int split = (c->precision == SOL_PRECISION_SPLIT && !c->barycentric) ? 1 : 0;
+  const int split = (c->precision != SOL_PRECISION_FP64 && !c->barycentric) ? 1 : 0;
   if (parts & 1) {
     const int nb_pre = (fc.npad + kPrepassBlock - 1) / kPrepassBlock;
     k_prepass<<<nb_pre, kPrepassBlock, 0, c->stream>>>(fc, d_y, split);
@@ -456,8 +773,14 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
     return SOL_OK;
   }
   if (split) {
-    k_gravity_ac<SOL_PRECISION_SPLIT><<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags,
-                                                                        &c->d_ctrl->dev_status);
+    const int nchunk = (c->n + kChunk - 1) / kChunk;
+    dim3 grid(nb, nchunk);
+    if (c->precision == SOL_PRECISION_SPLIT_FF)
+      k_pairs<SOL_PRECISION_SPLIT_FF><<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status);
+    else
+      k_pairs<SOL_PRECISION_SPLIT><<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status);
+    SOL_LAUNCHED();
+    k_combine<<<(c->n + 255) / 256, 256, 0, c->stream>>>(fc, d_y, d_dydt, c->d_part, nchunk, ts, flags);
   } else {
     k_gravity_ac<SOL_PRECISION_FP64><<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags,
                                                                        &c->d_ctrl->dev_status);
@@ -471,6 +794,7 @@ int sol_force_launch(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts,
 }
 
 int sol_force_tile() { return kTile; }
+int sol_force_part_doubles(int npad) { return ((npad + kChunk - 1) / kChunk) * PART_SLOTS * npad; }
 int sol_force_prepass_blocks(int npad) { return (npad + kPrepassBlock - 1) / kPrepassBlock; }
 
 // ---- caller-allocated variant ---------------------------------------------------

@@ -11,6 +11,7 @@
 // only reads the control block to decide whether to launch another attempt.
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "sol_internal.cuh"
 
@@ -71,7 +72,7 @@ __global__ void k_rkf78_final(int nv, const double* __restrict__ y0, Rkf78FinalA
     double e = h * fabs(f0 + f10 - fa.f[11][i] - fa.f[12][i]) * 41.0 / 840.0;
     err[i] = e;
     double q = fabs(e / ys[i]);
-    m = (q > m || q != q) ? q : m;  // a NaN propagates into the norm
+    m = q > m ? q : m;  // as GetErrorMax: a NaN entry never replaces the maximum
   }
   __shared__ double red[kBlock];
   red[threadIdx.x] = m;
@@ -79,7 +80,7 @@ __global__ void k_rkf78_final(int nv, const double* __restrict__ y0, Rkf78FinalA
   for (int w = kBlock / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
       double o = red[threadIdx.x + w];
-      if (o > red[threadIdx.x] || o != o) red[threadIdx.x] = o;
+      if (o > red[threadIdx.x]) red[threadIdx.x] = o;
     }
     __syncthreads();
   }
@@ -92,22 +93,28 @@ __global__ void k_reduce_max(const double* __restrict__ partial, int np, sol_ctr
   double m = 0.0;
   for (int b = threadIdx.x; b < np; b += blockDim.x) {
     double o = partial[b];
-    if (o > m || o != o) m = o;
+    if (o > m) m = o;
   }
   red[threadIdx.x] = m;
   __syncthreads();
   for (int w = kBlock / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
       double o = red[threadIdx.x + w];
-      if (o > red[threadIdx.x] || o != o) red[threadIdx.x] = o;
+      if (o > red[threadIdx.x]) red[threadIdx.x] = o;
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) ctrl->error_max = divide_eps ? red[0] / ctrl->eps : red[0];
 }
 
+// Keep iterating the device-side attempt loop while no attempt has been
+// accepted and no error has been raised.
+__device__ __forceinline__ void set_loop_condition(const sol_ctrl* c, cudaGraphConditionalHandle h, int use) {
+  if (use) cudaGraphSetConditional(h, (!c->accepted && c->dev_status == 0) ? 1u : 0u);
+}
+
 // Step-size control of RungeKuttaFehlberg78::Driver (:98-133).
-__global__ void k_control_rkf78(sol_ctrl* c) {
+__global__ void k_control_rkf78(sol_ctrl* c, cudaGraphConditionalHandle hcond, int use_cond) {
   const double em = c->error_max;
   const double h = c->h;
   if (em < 1.0) {
@@ -117,18 +124,15 @@ __global__ void k_control_rkf78(sol_ctrl* c) {
     c->h = c->h_next;
     c->accepted = 1;
     c->n_accepted++;
-    return;
+  } else {
+    c->n_rejected++;
+    double hTemp = 0.9 * h * pow(em, -0.25);
+    double hn = fabs(hTemp) > fabs(0.1 * h) ? hTemp : 0.1 * h;
+    c->h = hn;
+    double tNew = c->t + hn;
+    if (tNew == c->t) c->dev_status |= SOL_DEV_UNDERFLOW;
   }
-  c->n_rejected++;
-  if (em != em) {  // non-finite error norm: stop instead of shrinking to underflow
-    c->dev_status |= SOL_DEV_UNDERFLOW;
-    return;
-  }
-  double hTemp = 0.9 * h * pow(em, -0.25);
-  double hn = fabs(hTemp) > fabs(0.1 * h) ? hTemp : 0.1 * h;
-  c->h = hn;
-  double tNew = c->t + hn;
-  if (tNew == c->t) c->dev_status |= SOL_DEV_UNDERFLOW;
+  set_loop_condition(c, hcond, use_cond);
 }
 
 // RungeKutta4::Driver bookkeeping (RungeKutta4.cpp:355-365)
@@ -140,11 +144,20 @@ __global__ void k_control_rk4(sol_ctrl* c) {
   c->n_accepted++;
 }
 
-// Begin a driver call: bodyData->h = timeLine->hNext (RungeKuttaFehlberg78.cpp:74-75)
-__global__ void k_begin_step(sol_ctrl* c) {
+// Begin a driver call: bodyData->h = timeLine->hNext (RungeKuttaFehlberg78.cpp:74-75).
+// In a graph it also arms the attempt loop, which does not run once an
+// earlier driver call has raised an error.
+__global__ void k_begin_step(sol_ctrl* c, cudaGraphConditionalHandle hcond, int use_cond) {
   c->h = c->h_next;
   c->accepted = 0;
   c->iter = 0;
+  set_loop_condition(c, hcond, use_cond);
+}
+
+// swap(y0, y) of an accepted driver call (RungeKuttaFehlberg78.cpp:132)
+__global__ void k_accept_copy(int nv, double* __restrict__ y0, const double* __restrict__ y, const sol_ctrl* c) {
+  if (!c->accepted) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) y0[i] = y[i];
 }
 
 // ---- Dormand-Prince RKN 7(6), DormandPrince::Step2 (:246-491) ---------------
@@ -190,7 +203,7 @@ __global__ void k_dp_final(int n, const double* __restrict__ y0, DpFinalArgs s, 
     y[nn + 3] = y0[nn + 3] + h * (s.bdh[0] * f0 + s.bdh[4] * f4 + s.bdh[5] * f5 + s.bdh[6] * f6 + s.bdh[7] * f7);
     err[nn + 3] = 0.0;
     double q2 = fabs(e);
-    m = (q2 > m || q2 != q2) ? q2 : m;
+    m = q2 > m ? q2 : m;
   }
   __shared__ double red[kBlock];
   red[threadIdx.x] = m;
@@ -198,7 +211,7 @@ __global__ void k_dp_final(int n, const double* __restrict__ y0, DpFinalArgs s, 
   for (int w = kBlock / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
       double o = red[threadIdx.x + w];
-      if (o > red[threadIdx.x] || o != o) red[threadIdx.x] = o;
+      if (o > red[threadIdx.x]) red[threadIdx.x] = o;
     }
     __syncthreads();
   }
@@ -206,7 +219,7 @@ __global__ void k_dp_final(int n, const double* __restrict__ y0, DpFinalArgs s, 
 }
 
 // DormandPrince::Driver loop condition and step update (:145-164)
-__global__ void k_control_dp(sol_ctrl* c) {
+__global__ void k_control_dp(sol_ctrl* c, cudaGraphConditionalHandle hcond, int use_cond) {
   const double em = c->error_max;
   const double h = c->h;
   c->iter++;
@@ -215,15 +228,14 @@ __global__ void k_control_dp(sol_ctrl* c) {
   if (em > c->eps && c->iter <= 10) {
     c->n_rejected++;
     c->h = c->h_next;  // the next attempt uses timeLine->hNext
-    return;
-  }
-  if (c->iter > 10) {
+  } else if (c->iter > 10) {
     c->dev_status |= SOL_DEV_MAXITER;
-    return;
+  } else {
+    c->t += c->h_did;
+    c->accepted = 1;
+    c->n_accepted++;
   }
-  c->t += c->h_did;
-  c->accepted = 1;
-  c->n_accepted++;
+  set_loop_condition(c, hcond, use_cond);
 }
 
 // RKF78 stage tableau (RungeKuttaFehlberg78.cpp:41-56): per stage, the k
@@ -353,7 +365,7 @@ int ctrl_status(sol_ctx* c) {
 }
 
 int rkf78_driver_step(sol_ctx* c) {
-  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl, 0, 0);
   SOL_LAUNCHED();
   // Driver: all evaluate flags on for the first evaluation (:77-82)
   RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
@@ -362,7 +374,7 @@ int rkf78_driver_step(sol_ctx* c) {
   SOL_LAUNCHED();
   for (int attempt = 0;; ++attempt) {
     RET(rkf78_attempt(c, c->d_y0, c->d_y, c->d_err));
-    k_control_rkf78<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+    k_control_rkf78<<<1, 1, 0, c->stream>>>(c->d_ctrl, 0, 0);
     SOL_LAUNCHED();
     RET(read_ctrl(c));
     RET(ctrl_status(c));
@@ -374,7 +386,7 @@ int rkf78_driver_step(sol_ctx* c) {
 
 int rk4_driver_step(sol_ctx* c) {
   // RungeKutta4::Driver / Step (RungeKutta4.cpp:20-129)
-  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl, 0, 0);
   SOL_LAUNCHED();
   RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
   const double a21 = 1.0 / 2.0, a32 = 1.0 / 2.0, a43 = 1.0;
@@ -466,15 +478,13 @@ int launch_dp_stage(sol_ctx* c, int k, const DpStageArgs& s) {
   return SOL_OK;
 }
 
-int dp_driver_step(sol_ctx* c) {
+// One DormandPrince::Step2 attempt: 8 stages, the final sums, the error and its norm.
+int dp_attempt(sol_ctx* c) {
   const DpTab& T = dp_tab();
-  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl);
-  SOL_LAUNCHED();
-  RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
   double* f[9];
   f[0] = c->d_accel;
   for (int k = 1; k < 9; ++k) f[k] = c->d_fk[k];
-  for (;;) {
+  {
     for (int k = 1; k < 9; ++k) {
       DpStageArgs s;
       memset(&s, 0, sizeof(s));
@@ -508,7 +518,17 @@ int dp_driver_step(sol_ctx* c) {
     SOL_LAUNCHED();
     k_reduce_max<<<1, kBlock, 0, c->stream>>>(c->d_partial, g, c->d_ctrl, 0);
     SOL_LAUNCHED();
-    k_control_dp<<<1, 1, 0, c->stream>>>(c->d_ctrl);
+  }
+  return SOL_OK;
+}
+
+int dp_driver_step(sol_ctx* c) {
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl, 0, 0);
+  SOL_LAUNCHED();
+  RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
+  for (;;) {
+    RET(dp_attempt(c));
+    k_control_dp<<<1, 1, 0, c->stream>>>(c->d_ctrl, 0, 0);
     SOL_LAUNCHED();
     RET(read_ctrl(c));
     RET(ctrl_status(c));
@@ -518,9 +538,113 @@ int dp_driver_step(sol_ctx* c) {
   return SOL_OK;
 }
 
+// ---- device-side driver loop: one CUDA graph per driver call ------------------
+// prologue (begin, first evaluation, yscale) -> WHILE (attempt, control) ->
+// accept copy.  The control kernel sets the WHILE condition, so rejected
+// attempts are retried on the device with no host round trip; the host only
+// launches the graph once per driver call and reads the control block at the
+// end of the whole sequence.
+struct CaptureGuard {  // kernels captured into a graph are counted when the graph runs
+  CaptureGuard() { sol_capture_begin(); }
+  ~CaptureGuard() { sol_capture_end(); }
+};
+
+int capture_deps(cudaStream_t st, std::vector<cudaGraphNode_t>& out) {
+  cudaStreamCaptureStatus cs;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  SOL_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+  out.assign(deps, deps + nd);
+  return SOL_OK;
+}
+
+int build_driver_graph(sol_ctx* c, int integrator, DriverGraph& G) {
+  CaptureGuard guard;
+  const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+  cudaGraph_t graph = nullptr;
+  SOL_CUDA(cudaGraphCreate(&graph, 0));
+  int rc = SOL_OK;
+  cudaGraphConditionalHandle hcond;
+  std::vector<cudaGraphNode_t> deps;
+  cudaGraph_t tmp = nullptr;
+  long long k0 = sol_capture_count();
+  auto fail = [&](int r) {
+    cudaStreamCaptureStatus cs;
+    if (cudaStreamIsCapturing(c->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      cudaGraph_t junk = nullptr;
+      cudaStreamEndCapture(c->stream, &junk);
+    }
+    cudaGetLastError();
+    cudaGraphDestroy(graph);
+    return r;
+  };
+  if (cudaGraphConditionalHandleCreate(&hcond, graph, 0, 0) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  // prologue
+  if (cudaStreamBeginCaptureToGraph(c->stream, graph, nullptr, nullptr, 0, mode) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl, hcond, 1);
+  sol_count_launch();
+  if ((rc = sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL))) return fail(rc);
+  if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78) {
+    k_yscale<<<grid_for(c->nv), kBlock, 0, c->stream>>>(c->nv, c->d_y0, c->d_accel, c->d_yscale, c->d_ctrl);
+    sol_count_launch();
+  }
+  if ((rc = capture_deps(c->stream, deps))) return fail(rc);
+  if (cudaStreamEndCapture(c->stream, &tmp) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  G.k_pro = (int)(sol_capture_count() - k0);
+  // attempt loop
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hcond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  if (cudaGraphAddNode(&cnode, graph, deps.data(), nullptr, deps.size(), &cp) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  k0 = sol_capture_count();
+  if (cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, mode) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78) {
+    if ((rc = rkf78_attempt(c, c->d_y0, c->d_y, c->d_err))) return fail(rc);
+    k_control_rkf78<<<1, 1, 0, c->stream>>>(c->d_ctrl, hcond, 1);
+  } else {
+    if ((rc = dp_attempt(c))) return fail(rc);
+    k_control_dp<<<1, 1, 0, c->stream>>>(c->d_ctrl, hcond, 1);
+  }
+  sol_count_launch();
+  if (cudaStreamEndCapture(c->stream, &tmp) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  G.k_body = (int)(sol_capture_count() - k0);
+  // epilogue
+  k0 = sol_capture_count();
+  if (cudaStreamBeginCaptureToGraph(c->stream, graph, &cnode, nullptr, 1, mode) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  k_accept_copy<<<grid_for(c->nv), kBlock, 0, c->stream>>>(c->nv, c->d_y0, c->d_y, c->d_ctrl);
+  sol_count_launch();
+  if (cudaStreamEndCapture(c->stream, &tmp) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  G.k_epi = (int)(sol_capture_count() - k0);
+  cudaGraphExec_t exec = nullptr;
+  if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) return fail(SOL_ERR_CUDA);
+  G.graph = graph;
+  G.exec = exec;
+  G.precision = c->precision;
+  G.valid = 1;
+  return SOL_OK;
+}
+
 }  // namespace
 
 int sol_integrator_run(sol_ctx* c, int integrator, int n_steps) {
+  const int gi = integrator == SOL_RUNGE_KUTTA_FEHLBERG78 ? 0 : (integrator == SOL_DORMAND_PRINCE ? 1 : -1);
+  if (gi >= 0 && c->device_loop && n_steps > 0) {
+    DriverGraph& G = c->graphs[gi];
+    if (G.valid && G.precision != c->precision) sol_graph_release(G);
+    if (!G.valid && build_driver_graph(c, integrator, G) != SOL_OK) {
+      c->device_loop = 0;  // graphs unavailable here: keep the host-driven loop
+      cudaGetLastError();
+    } else {
+      for (int s = 0; s < n_steps; ++s) SOL_CUDA(cudaGraphLaunch(G.exec, c->stream));
+      c->graph_steps += n_steps;
+      c->graph_used = gi + 1;
+      return SOL_OK;
+    }
+  }
   for (int s = 0; s < n_steps; ++s) {
     int r;
     if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78) r = rkf78_driver_step(c);
@@ -557,3 +681,9 @@ int sol_rkf78_single_attempt(sol_ctx* c, double t, double h, const double* d_y0,
 }
 
 int sol_integrate_partials_needed(int nv) { return grid_for(nv); }
+
+void sol_graph_release(DriverGraph& G) {
+  if (G.exec) cudaGraphExecDestroy(G.exec);
+  if (G.graph) cudaGraphDestroy(G.graph);
+  G = DriverGraph{};
+}

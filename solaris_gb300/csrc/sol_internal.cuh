@@ -118,6 +118,19 @@ struct ForceCtx {
   int has_mig1, has_mig2;
 };
 
+// A captured driver call (RKF78 or DP) with its device-side attempt loop.
+struct DriverGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int precision = -1;
+  int valid = 0;
+  int k_pro = 0, k_body = 0, k_epi = 0;  // kernels per prologue / attempt / epilogue
+};
+void sol_graph_release(DriverGraph& G);
+void sol_capture_begin();
+void sol_capture_end();
+long long sol_capture_count();
+
 struct sol_ctx {
   int device;
   cudaStream_t stream;
@@ -139,12 +152,17 @@ struct sol_ctx {
   double *d_y0, *d_y, *d_accel, *d_yscale, *d_err, *d_ytmp, *d_fk[13];
   double *d_io_in, *d_io_out;  // boundary staging for host-buffer calls
   double* d_partial;           // block partial maxima of the error norm
+  double* d_part;              // per-chunk partial sums of the split pair kernels
   int n_partial;
   sol_ctrl* d_ctrl;
   sol_ctrl* h_ctrl;            // pinned mirror
   double* h_stage;             // pinned staging (max(6N, 3N) doubles)
   int state_valid;
   int last_eval_valid;
+  int device_loop;         // RKF78 / DP attempts looped on the device (CUDA graph)
+  DriverGraph graphs[2];   // [0] RKF78, [1] DP
+  long long graph_steps;   // driver calls run as graphs since the last sol_driver
+  int graph_used;
 };
 
 // ---- launch helpers (defined in sol_force.cu / sol_integrate.cu) --------------

@@ -58,6 +58,9 @@ class Context:
     def set_eval_flags(self, flags: int):
         abi.check(self.lib, self.lib.sol_set_eval_flags(self.h, int(flags)))
 
+    def set_device_loop(self, enable: bool):
+        abi.check(self.lib, self.lib.sol_set_device_loop(self.h, int(bool(enable))))
+
     def set_tolerance(self, eps: float):
         abi.check(self.lib, self.lib.sol_set_tolerance(self.h, float(eps)))
 

