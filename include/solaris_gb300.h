@@ -238,6 +238,30 @@ int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double c
 /* ---- diagnostics: Calculate::Integrals (Solaris/Calculate.cpp:43-62). --- */
 int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
 
+/* ---- batched ensembles ---------------------------------------------------
+ * Many independent systems (no nebula, heliocentric), each advanced by its
+ * own adaptive RungeKuttaFehlberg78 driver calls (RungeKuttaFehlberg78.cpp:
+ * 66-262) in one persistent launch: a CTA runs whole driver calls of one
+ * system at a time, taking systems from a work queue.  State is the
+ * concatenation of the systems' y[6N] arrays in the order given. */
+typedef struct sol_ensemble sol_ensemble;
+int sol_ensemble_create(const sol_body_data* systems, int32_t n_systems, int32_t device, sol_ensemble** out);
+int sol_ensemble_destroy(sol_ensemble* ens);
+/* SOL_PRECISION_FP64 (the reference's arithmetic) or SOL_PRECISION_SPLIT_FF */
+int sol_ensemble_set_precision(sol_ensemble* ens, int32_t precision);
+int sol_ensemble_set_tolerance(sol_ensemble* ens, double epsilon);
+int sol_ensemble_set_state(sol_ensemble* ens, const double* y0_all, const sol_time_line* time_lines);
+/* any output may be NULL; status[s] is SOL_OK or SOL_ERR_UNDERFLOW per system */
+int sol_ensemble_get_state(sol_ensemble* ens, double* y0_all, sol_time_line* time_lines, int32_t* status);
+/* n_steps driver calls for every system */
+int sol_ensemble_advance(sol_ensemble* ens, int32_t n_steps, sol_step_stats* stats);
+/* launch shape: threads per system (multiple of 32) and resident systems per SM */
+int sol_ensemble_configure(sol_ensemble* ens, int32_t threads_per_system, int32_t systems_per_sm);
+/* times `steps` driver calls for each candidate launch shape on a copy of the
+ * state, restores the state and keeps the fastest shape */
+int sol_ensemble_autotune(sol_ensemble* ens, int32_t steps, int32_t* threads_per_system, int32_t* systems_per_sm,
+                          double* best_ms);
+
 /* ---- caller-allocated force evaluation --------------------------------- */
 /* GravityAC alone (no gas terms) for callers that cannot allocate device
  * memory: a host framework that owns every device byte, a plugin with a fixed

@@ -179,6 +179,16 @@ def _declare(lib):
         "sol_kernel_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
         "sol_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
         "sol_bench_force": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
+        "sol_ensemble_create": (C.c_int, [C.POINTER(SolBodyData), C.c_int32, C.c_int32, C.POINTER(P)]),
+        "sol_ensemble_destroy": (C.c_int, [P]),
+        "sol_ensemble_set_precision": (C.c_int, [P, C.c_int32]),
+        "sol_ensemble_set_tolerance": (C.c_int, [P, C.c_double]),
+        "sol_ensemble_set_state": (C.c_int, [P, _PF64, C.POINTER(SolTimeLine)]),
+        "sol_ensemble_get_state": (C.c_int, [P, _PF64, C.POINTER(SolTimeLine), _PI32]),
+        "sol_ensemble_advance": (C.c_int, [P, C.c_int32, C.POINTER(SolStepStats)]),
+        "sol_ensemble_configure": (C.c_int, [P, C.c_int32, C.c_int32]),
+        "sol_ensemble_autotune": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_double)]),
         "sol_gravity_noalloc": (C.c_int, [C.POINTER(SolNBodies), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     }
@@ -196,7 +206,10 @@ def exported_names():
         "sol_set_precision", "sol_set_eval_flags", "sol_get_n_total", "sol_accel_compute", "sol_get_mig_type",
         "sol_set_state", "sol_get_state", "sol_set_tolerance", "sol_set_device_loop", "sol_driver", "sol_driver_host",
         "sol_rkf78_step", "sol_get_last_eval", "sol_check_events", "sol_integrals", "sol_measure_fp64_peak",
-        "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc"]
+        "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc",
+        "sol_ensemble_create", "sol_ensemble_destroy", "sol_ensemble_set_precision", "sol_ensemble_set_tolerance",
+        "sol_ensemble_set_state", "sol_ensemble_get_state", "sol_ensemble_advance", "sol_ensemble_configure",
+        "sol_ensemble_autotune"]
 
 
 def load_library(path: str | None = None):

@@ -139,6 +139,71 @@ class Context:
         return out
 
 
+class Ensemble:
+    """Many independent systems advanced in one persistent launch
+    (sol_ensemble_*): each system runs its own adaptive RKF78 driver calls."""
+
+    def __init__(self, systems, device: int = 0, precision: int = abi.PRECISION_FP64, epsilon: float = 1e-10):
+        self.lib = abi.load_library()
+        self.systems = systems
+        self._views = [abi.BodyDataView(s) for s in systems]
+        arr = (abi.SolBodyData * len(systems))(*[v.struct for v in self._views])
+        self._arr = arr
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.sol_ensemble_create(arr, len(systems), int(device), C.byref(h)))
+        self.h = h
+        self.offsets = np.cumsum([0] + [s.n for s in systems])
+        abi.check(self.lib, self.lib.sol_ensemble_set_precision(self.h, int(precision)))
+        abi.check(self.lib, self.lib.sol_ensemble_set_tolerance(self.h, float(epsilon)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sol_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_precision(self, p):
+        abi.check(self.lib, self.lib.sol_ensemble_set_precision(self.h, int(p)))
+
+    def set_state(self, y0s, times, h_next):
+        y = np.ascontiguousarray(np.concatenate([np.asarray(v, np.float64) for v in y0s]))
+        tls = (abi.SolTimeLine * len(self.systems))(*[abi.SolTimeLine(float(t), float(h), 0.0)
+                                                     for t, h in zip(times, h_next)])
+        abi.check(self.lib, self.lib.sol_ensemble_set_state(self.h, abi.f64p(y), tls))
+
+    def get_state(self):
+        y = np.empty(6 * int(self.offsets[-1]))
+        tls = (abi.SolTimeLine * len(self.systems))()
+        st = np.zeros(len(self.systems), np.int32)
+        abi.check(self.lib, self.lib.sol_ensemble_get_state(self.h, abi.f64p(y), tls, abi.i32p(st)))
+        ys = [y[6 * self.offsets[k]:6 * self.offsets[k + 1]] for k in range(len(self.systems))]
+        return ys, [(t.time, t.h_next, t.h_did) for t in tls], st
+
+    def advance(self, n_steps):
+        st = abi.SolStepStats()
+        abi.check(self.lib, self.lib.sol_ensemble_advance(self.h, int(n_steps), C.byref(st)))
+        return st.accepted, st.rejected, st.evaluations
+
+    def configure(self, threads, per_sm):
+        abi.check(self.lib, self.lib.sol_ensemble_configure(self.h, int(threads), int(per_sm)))
+
+    def autotune(self, steps=1):
+        b, p, ms = C.c_int32(0), C.c_int32(0), C.c_double(0)
+        abi.check(self.lib, self.lib.sol_ensemble_autotune(self.h, int(steps), C.byref(b), C.byref(p), C.byref(ms)))
+        return b.value, p.value, ms.value
+
+
 def kernel_launches() -> int:
     lib = abi.load_library()
     v = C.c_int64(0)

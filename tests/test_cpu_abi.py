@@ -100,3 +100,15 @@ def test_pair_count_matches_oracle_sample():
     assert s3.pair_count() == 299 + 299 * 298
     o3 = oracle.Oracle(s3)
     assert o3.gravity_sample(s3.y0, 1, s3.n)[1] == s3.pair_count()
+
+
+def test_ensemble_rejects_unsorted_system(lib):
+    s = scenarios.config3(n=17)
+    t = scenarios.config3(n=9)
+    t.type = t.type.copy()
+    t.type[3] = abi.TEST_PARTICLE
+    views = [abi.BodyDataView(x) for x in (s, t)]
+    arr = (abi.SolBodyData * 2)(*[v.struct for v in views])
+    h = C.c_void_p()
+    assert lib.sol_ensemble_create(arr, 2, 0, C.byref(h)) == abi.SOL_ERR_ARG
+    assert b"system 1" in lib.sol_last_error()
