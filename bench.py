@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_BODIES, help=argparse.SUPPRESS)
+    ap.add_argument("--skip-ensemble", action="store_true", help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -146,6 +147,50 @@ def traffic_from_profiles():
             except ValueError:
                 return None
     return None
+
+
+def ensemble_section(local):
+    """Batched-ensemble figures (4,096 systems of 1 star + 2..12 planets +
+    0..512 test particles, adaptive RKF78 eps 1e-10): system-steps/s of the
+    persistent ensemble kernel (SPLIT_FF and FP64, launch shape autotuned),
+    of serial per-system launches of the single-system path, and of the CPU
+    oracle on one core."""
+    import oracle
+    from solaris_gb300 import abi, engine, scenarios
+    systems = scenarios.config4()
+    out = {"workload": "4096 systems: 1 star + U{2..12} planets + U{0..512} test particles, RKF78 eps 1e-10",
+           "unit": "system-steps/s", "bodies": int(sum(x.n for x in systems))}
+    steps = 10
+    for name, prec in (("split_ff", abi.PRECISION_SPLIT_FF), ("fp64", abi.PRECISION_FP64)):
+        with engine.Ensemble(systems, device=local, precision=prec) as ens:
+            ens.set_state([x.y0 for x in systems], [0.0] * len(systems), [x.h0 for x in systems])
+            threads, per_sm, _ = ens.autotune(steps=2)
+            ens.advance(2)
+            t0 = time.perf_counter()
+            acc, rej, _ = ens.advance(steps)
+            dt = time.perf_counter() - t0
+            out[name] = {"value": acc / dt, "accepted": acc, "rejected": rej, "threads_per_system": threads,
+                         "systems_per_sm": per_sm}
+    k, acc_tot, dt_tot = 16, 0, 0.0
+    for x in systems[:k]:
+        with engine.Context(x, device=local) as ctx:
+            ctx.set_state(x.y0)
+            ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0.0, x.h0, 2)
+            t0 = time.perf_counter()
+            r = ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0.0, x.h0, steps)
+            dt_tot += time.perf_counter() - t0
+            acc_tot += r["stats"][0]
+    out["serial_single_system"] = {"value": acc_tot / dt_tot, "sample_systems": k}
+    out["speedup_vs_serial"] = out["split_ff"]["value"] / out["serial_single_system"]["value"]
+    k, acc_tot, dt_tot = 8, 0, 0.0
+    for x in systems[:k]:
+        o = oracle.Oracle(x)
+        t0 = time.perf_counter()
+        r = o.driver(abi.RUNGE_KUTTA_FEHLBERG78, x.y0, 0.0, x.h0, steps)
+        dt_tot += time.perf_counter() - t0
+        acc_tot += r["stats"][0]
+    out["cpu_port_1_core"] = {"value": acc_tot / dt_tot, "sample_systems": k, "kind": "port", "cores": 1}
+    return out
 
 
 def main():
@@ -263,6 +308,7 @@ def main():
         if name in acc:
             forms[name]["max_rel_accel_err"], forms[name]["rms_rel_accel_err"] = acc[name]
     pps_head = pairs_eval / (ms_launch[head_name] * 1e-3)
+    ensemble = ensemble_section(local) if not args.skip_ensemble else None
     cpu = None
     if rank == 0:
         n_sinks = 12288
@@ -294,6 +340,7 @@ def main():
                 "steps": ke, "api": "sol_driver_host (pinned host y0 in/out)"},
         "gpu_launches": head["launches"],
         "clocks": head["clocks"],
+        "ensemble": ensemble,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -238,6 +238,19 @@ int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double c
 /* ---- diagnostics: Calculate::Integrals (Solaris/Calculate.cpp:43-62). --- */
 int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
 
+/* ---- discrete adjoint of fixed-step RKF78 --------------------------------
+ * Forward: n_steps RungeKuttaFehlberg78::Step calls at constant h, each taking
+ * the 7th-order result (RungeKuttaFehlberg78.cpp:147-250; heliocentric
+ * gravity, no nebula), the state stored every `checkpoint_every` steps.
+ * Backward: given dL/dy at the final state, dL/dy0 (6N) and dL/dmass (N) of
+ * that discrete map, recomputing each segment from its checkpoint.  A
+ * torch.autograd.Function-style pair: forward once, then backward. */
+int sol_adjoint_forward(sol_ctx* ctx, double h, int32_t n_steps, int32_t checkpoint_every, const double* y0,
+                        double* y_final);
+int sol_adjoint_backward(sol_ctx* ctx, const double* dl_dy_final, double* dl_dy0, double* dl_dmass);
+/* Replace the body masses (BodyData::mass) of a context. */
+int sol_set_masses(sol_ctx* ctx, const double* mass);
+
 /* ---- batched ensembles ---------------------------------------------------
  * Many independent systems (no nebula, heliocentric), each advanced by its
  * own adaptive RungeKuttaFehlberg78 driver calls (RungeKuttaFehlberg78.cpp:

@@ -72,6 +72,9 @@ def load():
         lib.orc_kepler_equation_solver.argtypes = [C.c_double, C.c_double, C.c_double, F]
         lib.orc_calculate_phase.argtypes = [C.c_double, F, F]
         lib.orc_calculate_orbital_element.argtypes = [C.c_double, F, F, F, C.c_int32]
+        lib.orc_jvp.argtypes = [P, F, F, F, F]
+        lib.orc_rkf78_fixed.argtypes = [P, F, C.c_double, C.c_int32, F, F, F, F]
+        lib.orc_set_masses.argtypes = [P, F]
         lib.orc_gravity_ac_sample.restype = C.c_int64
         lib.orc_gravity_ac_sample.argtypes = [P, F, C.c_int32, C.c_int32, F, C.c_int32]
         _lib = lib
@@ -146,6 +149,26 @@ class Oracle:
         out = np.zeros(16)
         self.lib.orc_integrals(self.h, abi.f64p(y0), abi.f64p(out))
         return out
+
+    def jvp(self, y, dy, dm=None):
+        y, dy = np.ascontiguousarray(y, np.float64), np.ascontiguousarray(dy, np.float64)
+        out = np.zeros(6 * self.n)
+        dmp = abi.f64p(np.ascontiguousarray(dm, np.float64)) if dm is not None else None
+        self.lib.orc_jvp(self.h, abi.f64p(y), abi.f64p(dy), dmp, abi.f64p(out))
+        return out
+
+    def set_masses(self, m):
+        m = np.ascontiguousarray(m, np.float64)
+        self.lib.orc_set_masses(self.h, abi.f64p(m))
+
+    def rkf78_fixed(self, y0, h, n_steps, dy0=None, dm=None):
+        y0 = np.ascontiguousarray(y0, np.float64)
+        y = np.zeros(6 * self.n)
+        dyo = np.zeros(6 * self.n)
+        dyp = abi.f64p(np.ascontiguousarray(dy0, np.float64)) if dy0 is not None else None
+        dmp = abi.f64p(np.ascontiguousarray(dm, np.float64)) if dm is not None else None
+        self.lib.orc_rkf78_fixed(self.h, abi.f64p(y0), h, n_steps, abi.f64p(y), dyp, dmp, abi.f64p(dyo))
+        return (y, dyo) if dy0 is not None else y
 
     def gravity_sample(self, y, i_begin, i_end, n_threads=1):
         y = np.ascontiguousarray(y, dtype=np.float64)

@@ -976,3 +976,166 @@ int64_t orc_gravity_ac_sample(orc_system* s, const double* y, int32_t i_begin, i
   }
   return pairs;
 }
+
+/* ---- fixed-step RKF78 and its tangent-linear model ----------------------
+ * Fixed-step integration: RungeKuttaFehlberg78::Step at constant h (no step
+ * control), y_{n+1} = its 7th-order result (RungeKuttaFehlberg78.cpp:236-238).
+ * Masses are variables of the tangent-linear model (the gradient with respect
+ * to masses is part of the adjoint's output); gas terms are not included. */
+
+/* T(x) v = v / |x|^3 - 3 x (x . v) / |x|^5 */
+static void tensor_apply(const double* x, const double* v, double* out) {
+  double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+  double r = sqrt(r2);
+  double r3 = r2 * r;
+  double r5 = r3 * r2;
+  double xv = x[0] * v[0] + x[1] * v[1] + x[2] * v[2];
+  for (int k = 0; k < 3; ++k) out[k] = v[k] / r3 - 3.0 * x[k] * xv / r5;
+}
+
+/* Jacobian-vector product of GravityAC (Acceleration.cpp:248-329):
+ * d(dydt) for a perturbation (dy, dm) at state y. */
+void orc_jvp(orc_system* s, const double* y, const double* dy, const double* dm, double* df) {
+  int N = s->total, nm = n_massive(s), nspl = s->n.super_planetesimal;
+  double m0 = s->mass[0], dm0 = dm ? dm[0] : 0.0;
+  for (int k = 0; k < 6; ++k) df[k] = 0.0;
+  for (int i = 1; i < N; ++i) {
+    const double* ri = &y[6 * i];
+    const double* dri = &dy[6 * i];
+    double* o = &df[6 * i];
+    o[0] = dri[3];
+    o[1] = dri[4];
+    o[2] = dri[5];
+    double r2 = ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
+    double rm3 = 1.0 / (r2 * sqrt(r2));
+    double t[3];
+    tensor_apply(ri, dri, t);
+    double mu = K_GAUSS2 * (m0 + s->mass[i]);
+    double dmu = K_GAUSS2 * (dm0 + (dm ? dm[i] : 0.0));
+    for (int k = 0; k < 3; ++k) o[3 + k] = -dmu * ri[k] * rm3 - mu * t[k];
+    int ns = s->type[i] <= SOL_PROTO_PLANET ? nm + nspl : nm;
+    for (int j = 1; j < ns; ++j) {
+      if (j == i) continue;
+      const double* rj = &y[6 * j];
+      const double* drj = &dy[6 * j];
+      double d[3] = {rj[0] - ri[0], rj[1] - ri[1], rj[2] - ri[2]};
+      double dd[3] = {drj[0] - dri[0], drj[1] - dri[1], drj[2] - dri[2]};
+      double d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      double dm3 = 1.0 / (d2 * sqrt(d2));
+      double rj2 = rj[0] * rj[0] + rj[1] * rj[1] + rj[2] * rj[2];
+      double rjm3 = 1.0 / (rj2 * sqrt(rj2));
+      double td[3], tr[3];
+      tensor_apply(d, dd, td);
+      tensor_apply(rj, drj, tr);
+      double gm = K_GAUSS2 * s->mass[j];
+      double gdm = K_GAUSS2 * (dm ? dm[j] : 0.0);
+      for (int k = 0; k < 3; ++k) o[3 + k] += gdm * (d[k] * dm3 - rj[k] * rjm3) + gm * (td[k] - tr[k]);
+    }
+  }
+}
+
+static void rkf78_fixed_stages(orc_system* s, const double* y0, double h, double* ynew, double** Y, double** F) {
+  /* stage states Y[0..12] and derivatives F[0..12] of one Step at fixed h */
+  const int nv = 6 * s->total;
+  const double A[13][13] = {
+      {0},
+      {2.0 / 27.0},
+      {1.0 / 36.0, 1.0 / 12.0},
+      {1.0 / 24.0, 0, 1.0 / 8.0},
+      {5.0 / 12.0, 0, -25.0 / 16.0, 25.0 / 16.0},
+      {1.0 / 20.0, 0, 0, 1.0 / 4.0, 1.0 / 5.0},
+      {-25.0 / 108.0, 0, 0, 125.0 / 108.0, -65.0 / 27.0, 125.0 / 54.0},
+      {31.0 / 300.0, 0, 0, 0, 61.0 / 225.0, -2.0 / 9.0, 13.0 / 900.0},
+      {2.0, 0, 0, -53.0 / 6.0, 704.0 / 45.0, -107.0 / 9.0, 67.0 / 90.0, 3.0},
+      {-91.0 / 108.0, 0, 0, 23.0 / 108.0, -976.0 / 135.0, 311.0 / 54.0, -19.0 / 60.0, 17.0 / 6.0, -1.0 / 12.0},
+      {2383.0 / 4100.0, 0, 0, -341.0 / 164.0, 4496.0 / 1025.0, -301.0 / 82.0, 2133.0 / 4100.0, 45.0 / 82.0,
+       45.0 / 164.0, 18.0 / 41.0},
+      {3.0 / 205.0, 0, 0, 0, 0, -6.0 / 41.0, -3.0 / 205.0, -3.0 / 41.0, 3.0 / 41.0, 6.0 / 41.0, 0},
+      {-1777.0 / 4100.0, 0, 0, -341.0 / 164.0, 4496.0 / 1025.0, -289.0 / 82.0, 2193.0 / 4100.0, 51.0 / 82.0,
+       33.0 / 164.0, 12.0 / 41.0, 0, 1.0}};
+  const double B[13] = {41.0 / 840.0, 0, 0, 0, 0, 34.0 / 105.0, 9.0 / 35.0, 9.0 / 35.0, 9.0 / 280.0, 9.0 / 280.0,
+                        41.0 / 840.0, 0, 0};
+  for (int r = 0; r < 13; ++r) {
+    for (int e = 0; e < nv; ++e) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += A[r][l] * F[l][e];
+      Y[r][e] = y0[e] + h * acc;
+    }
+    s->eval_drag = s->eval_mig1 = s->eval_mig2 = 0;
+    orc_compute(s, 0.0, Y[r], F[r]);
+  }
+  for (int e = 0; e < nv; ++e) {
+    double acc = 0.0;
+    for (int k = 0; k < 13; ++k) acc += B[k] * F[k][e];
+    ynew[e] = y0[e] + h * acc;
+  }
+}
+
+/* n fixed steps from y0; with dy0/dm also the tangent-linear solution dy. */
+int orc_rkf78_fixed(orc_system* s, const double* y0, double h, int32_t n_steps, double* y_out, const double* dy0,
+                    const double* dm, double* dy_out) {
+  const int nv = 6 * s->total;
+  double *Y[13], *F[13], *dY[13], *dF[13];
+  for (int k = 0; k < 13; ++k) {
+    Y[k] = (double*)malloc(sizeof(double) * nv);
+    F[k] = (double*)malloc(sizeof(double) * nv);
+    dY[k] = (double*)malloc(sizeof(double) * nv);
+    dF[k] = (double*)malloc(sizeof(double) * nv);
+  }
+  double* y = (double*)malloc(sizeof(double) * nv);
+  double* yn = (double*)malloc(sizeof(double) * nv);
+  double* dy = (double*)malloc(sizeof(double) * nv);
+  memcpy(y, y0, sizeof(double) * nv);
+  if (dy0) memcpy(dy, dy0, sizeof(double) * nv);
+  const double A[13][13] = {
+      {0},
+      {2.0 / 27.0},
+      {1.0 / 36.0, 1.0 / 12.0},
+      {1.0 / 24.0, 0, 1.0 / 8.0},
+      {5.0 / 12.0, 0, -25.0 / 16.0, 25.0 / 16.0},
+      {1.0 / 20.0, 0, 0, 1.0 / 4.0, 1.0 / 5.0},
+      {-25.0 / 108.0, 0, 0, 125.0 / 108.0, -65.0 / 27.0, 125.0 / 54.0},
+      {31.0 / 300.0, 0, 0, 0, 61.0 / 225.0, -2.0 / 9.0, 13.0 / 900.0},
+      {2.0, 0, 0, -53.0 / 6.0, 704.0 / 45.0, -107.0 / 9.0, 67.0 / 90.0, 3.0},
+      {-91.0 / 108.0, 0, 0, 23.0 / 108.0, -976.0 / 135.0, 311.0 / 54.0, -19.0 / 60.0, 17.0 / 6.0, -1.0 / 12.0},
+      {2383.0 / 4100.0, 0, 0, -341.0 / 164.0, 4496.0 / 1025.0, -301.0 / 82.0, 2133.0 / 4100.0, 45.0 / 82.0,
+       45.0 / 164.0, 18.0 / 41.0},
+      {3.0 / 205.0, 0, 0, 0, 0, -6.0 / 41.0, -3.0 / 205.0, -3.0 / 41.0, 3.0 / 41.0, 6.0 / 41.0, 0},
+      {-1777.0 / 4100.0, 0, 0, -341.0 / 164.0, 4496.0 / 1025.0, -289.0 / 82.0, 2193.0 / 4100.0, 51.0 / 82.0,
+       33.0 / 164.0, 12.0 / 41.0, 0, 1.0}};
+  const double B[13] = {41.0 / 840.0, 0, 0, 0, 0, 34.0 / 105.0, 9.0 / 35.0, 9.0 / 35.0, 9.0 / 280.0, 9.0 / 280.0,
+                        41.0 / 840.0, 0, 0};
+  for (int n = 0; n < n_steps; ++n) {
+    rkf78_fixed_stages(s, y, h, yn, Y, F);
+    if (dy0) {
+      for (int r = 0; r < 13; ++r) {
+        for (int e = 0; e < nv; ++e) {
+          double acc = 0.0;
+          for (int l = 0; l < r; ++l) acc += A[r][l] * dF[l][e];
+          dY[r][e] = dy[e] + h * acc;
+        }
+        orc_jvp(s, Y[r], dY[r], dm, dF[r]);
+      }
+      for (int e = 0; e < nv; ++e) {
+        double acc = 0.0;
+        for (int k = 0; k < 13; ++k) acc += B[k] * dF[k][e];
+        dy[e] = dy[e] + h * acc;
+      }
+    }
+    memcpy(y, yn, sizeof(double) * nv);
+  }
+  memcpy(y_out, y, sizeof(double) * nv);
+  if (dy0 && dy_out) memcpy(dy_out, dy, sizeof(double) * nv);
+  for (int k = 0; k < 13; ++k) {
+    free(Y[k]);
+    free(F[k]);
+    free(dY[k]);
+    free(dF[k]);
+  }
+  free(y);
+  free(yn);
+  free(dy);
+  return 0;
+}
+
+void orc_set_masses(orc_system* s, const double* mass) { memcpy(s->mass, mass, sizeof(double) * s->total); }

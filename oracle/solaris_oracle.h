@@ -58,6 +58,14 @@ int orc_calculate_orbital_element(double mu, const double phase[6], double* a, d
 int64_t orc_gravity_ac_sample(orc_system* s, const double* y, int32_t i_begin, int32_t i_end,
                               double* dydt, int32_t n_threads);
 
+/* Jacobian-vector product of GravityAC for a perturbation (dy, dm). */
+void orc_jvp(orc_system* s, const double* y, const double* dy, const double* dm, double* df);
+/* n fixed-h RKF78 steps (7th-order result); with dy0 (and dm) also the
+ * tangent-linear solution. */
+int orc_rkf78_fixed(orc_system* s, const double* y0, double h, int32_t n_steps, double* y_out, const double* dy0,
+                    const double* dm, double* dy_out);
+void orc_set_masses(orc_system* s, const double* mass);
+
 #ifdef __cplusplus
 }
 #endif

@@ -179,6 +179,9 @@ def _declare(lib):
         "sol_kernel_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
         "sol_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
         "sol_bench_force": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
+        "sol_adjoint_forward": (C.c_int, [P, C.c_double, C.c_int32, C.c_int32, _PF64, _PF64]),
+        "sol_adjoint_backward": (C.c_int, [P, _PF64, _PF64, _PF64]),
+        "sol_set_masses": (C.c_int, [P, _PF64]),
         "sol_ensemble_create": (C.c_int, [C.POINTER(SolBodyData), C.c_int32, C.c_int32, C.POINTER(P)]),
         "sol_ensemble_destroy": (C.c_int, [P]),
         "sol_ensemble_set_precision": (C.c_int, [P, C.c_int32]),
@@ -209,7 +212,7 @@ def exported_names():
         "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc",
         "sol_ensemble_create", "sol_ensemble_destroy", "sol_ensemble_set_precision", "sol_ensemble_set_tolerance",
         "sol_ensemble_set_state", "sol_ensemble_get_state", "sol_ensemble_advance", "sol_ensemble_configure",
-        "sol_ensemble_autotune"]
+        "sol_ensemble_autotune", "sol_adjoint_forward", "sol_adjoint_backward", "sol_set_masses"]
 
 
 def load_library(path: str | None = None):

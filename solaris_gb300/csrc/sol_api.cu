@@ -143,6 +143,7 @@ void free_ctx(sol_ctx* c) {
   for (int k = 0; k < 13; ++k)
     if (c->d_fk[k]) cudaFree(c->d_fk[k]);
   for (int k = 0; k < 2; ++k) sol_graph_release(c->graphs[k]);
+  sol_adjoint_free(c->adj);
   if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->stream) cudaStreamDestroy(c->stream);

@@ -87,6 +87,17 @@ __global__ void k_rkf78_final(int nv, const double* __restrict__ y0, Rkf78FinalA
   if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
+// The 7th-order result alone (RungeKuttaFehlberg78.cpp:236-238)
+__global__ void k_rkf78_y(int nv, const double* __restrict__ y0, Rkf78FinalArgs fa, double* __restrict__ y,
+                          const sol_ctrl* ctrl) {
+  const double h = ctrl->h;
+  const double D1_0 = 41.0 / 840.0, D1_5 = 34.0 / 105.0, D1_6 = 9.0 / 35.0, D1_8 = 9.0 / 280.0,
+               D1_10 = 41.0 / 840.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x)
+    y[i] = y0[i] + h * (D1_0 * fa.f[0][i] + D1_5 * fa.f[5][i] + D1_6 * (fa.f[6][i] + fa.f[7][i]) +
+                        D1_8 * (fa.f[8][i] + fa.f[9][i]) + D1_10 * fa.f[10][i]);
+}
+
 // max over block partials -> ctrl->error_max (divided by eps for RKF78)
 __global__ void k_reduce_max(const double* __restrict__ partial, int np, sol_ctrl* ctrl, int divide_eps) {
   __shared__ double red[kBlock];
@@ -681,6 +692,36 @@ int sol_rkf78_single_attempt(sol_ctx* c, double t, double h, const double* d_y0,
 }
 
 int sol_integrate_partials_needed(int nv) { return grid_for(nv); }
+
+// One fixed-h RungeKuttaFehlberg78::Step without the error estimate: the first
+// evaluation at y0, 12 stages and the 7th-order result into y.  Stage inputs go
+// to stage_out[r] when given (r = 1..12), else to the context's scratch.  h is
+// the control block's.
+int sol_rkf78_stages(sol_ctx* c, const double* d_y0, double* d_y, double* const* stage_out) {
+  const Rkf78Stage* st = rkf78_stages();
+  double* fk[13];
+  fk[0] = c->d_accel;
+  for (int k = 1; k < 13; ++k) fk[k] = c->d_fk[k];
+  RET(sol_force_launch(c, d_y0, fk[0], stage_time(c, 0.0), SOL_EVAL_ALL));
+  for (int r = 1; r <= 12; ++r) {
+    StageArgs sa;
+    memset(&sa, 0, sizeof(sa));
+    for (int k = 0; k < st[r].k; ++k) {
+      sa.f[k] = fk[st[r].idx[k]];
+      sa.a[k] = st[r].a[k];
+    }
+    if (r > 10) break;  // stages 11 and 12 enter only the error estimate
+    double* out = (stage_out && stage_out[r]) ? stage_out[r] : c->d_ytmp;
+    RET(launch_stage(c, st[r].k, sa, d_y0, out));
+    RET(sol_force_launch(c, out, fk[r], stage_time(c, 0.0), SOL_EVAL_GAS_DRAG));
+  }
+  Rkf78FinalArgs fa;
+  for (int k = 0; k < 13; ++k) fa.f[k] = fk[k];
+  const int g = grid_for(c->nv);
+  k_rkf78_y<<<g, kBlock, 0, c->stream>>>(c->nv, d_y0, fa, d_y, c->d_ctrl);
+  SOL_LAUNCHED();
+  return SOL_OK;
+}
 
 void sol_graph_release(DriverGraph& G) {
   if (G.exec) cudaGraphExecDestroy(G.exec);

@@ -131,6 +131,9 @@ void sol_capture_begin();
 void sol_capture_end();
 long long sol_capture_count();
 
+struct sol_adjoint_state;
+void sol_adjoint_free(sol_adjoint_state* a);
+
 struct sol_ctx {
   int device;
   cudaStream_t stream;
@@ -163,6 +166,7 @@ struct sol_ctx {
   DriverGraph graphs[2];   // [0] RKF78, [1] DP
   long long graph_steps;   // driver calls run as graphs since the last sol_driver
   int graph_used;
+  sol_adjoint_state* adj;  // checkpoints and buffers of the discrete adjoint
 };
 
 // ---- launch helpers (defined in sol_force.cu / sol_integrate.cu) --------------

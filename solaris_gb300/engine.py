@@ -121,6 +121,24 @@ class Context:
         abi.check(self.lib, self.lib.sol_bench_force(self.h, int(precision), int(reps), C.byref(ms)))
         return float(ms.value)
 
+    # -- discrete adjoint ---------------------------------------------------------
+    def set_masses(self, mass):
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        abi.check(self.lib, self.lib.sol_set_masses(self.h, abi.f64p(m)))
+
+    def adjoint_forward(self, y0, h, n_steps, checkpoint_every=100):
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        y = np.empty(6 * self.n)
+        abi.check(self.lib, self.lib.sol_adjoint_forward(self.h, float(h), int(n_steps), int(checkpoint_every),
+                                                         abi.f64p(y0), abi.f64p(y)))
+        return y
+
+    def adjoint_backward(self, dl_dy_final):
+        g = np.ascontiguousarray(dl_dy_final, dtype=np.float64)
+        dy0, dm = np.empty(6 * self.n), np.empty(self.n)
+        abi.check(self.lib, self.lib.sol_adjoint_backward(self.h, abi.f64p(g), abi.f64p(dy0), abi.f64p(dm)))
+        return dy0, dm
+
     # -- events and integrals ----------------------------------------------------
     def events(self, ejection, hit_centrum, collision_factor, capacity=4096):
         ev = (abi.SolEvent * max(capacity, 1))()
