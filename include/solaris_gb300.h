@@ -230,6 +230,66 @@ int sol_rkf78_step(sol_ctx* ctx, double t, double h, const double* y0, double* y
 /* Per-body outputs of the last force evaluation (rm3, NN arrays). */
 int sol_get_last_eval(sol_ctx* ctx, double* rm3, int32_t* nn_idx, double* nn_dist);
 
+/* ---- the remaining public members of Acceleration and the integrators ----
+ * (Solaris/Acceleration.h:17-45, RungeKuttaFehlberg78.h:17-24,
+ * RungeKutta4.h:11-17, DormandPrince.h:10-18), used by the C++ class facade
+ * (solaris_gb300/facade). */
+enum sol_term {
+  SOL_TERM_GRAVITY = 0,  /* GravityAC / GravityBC (Acceleration.cpp:248-329, :541-634) */
+  SOL_TERM_GAS_DRAG = 1, /* GasDragAC / GasDragBC (:331-422) */
+  SOL_TERM_TYPE_I = 2,   /* MigrationTypeIAC / MigrationTypeIBC (:424-485) */
+  SOL_TERM_TYPE_II = 3   /* MigrationTypeIIAC / MigrationTypeIIBC (:487-528) */
+};
+/* One term of Acceleration::Compute on host buffers, in the context's frame.
+ * GRAVITY: out[6N] (velocities and gravity, no nebula terms); rm3 and the NN
+ *   arrays are then those of this evaluation (sol_get_last_eval).
+ * GAS_DRAG: out[3 (superPlanetesimal + planetesimal)], rows of the bodies
+ *   from NOfMassive on.
+ * TYPE_I: out[3 (rockyPlanet + protoPlanet)], rows of the bodies from
+ *   centralBody + giantPlanet on; TYPE_II: out[3 giantPlanet], rows from
+ *   centralBody on.  Rows of bodies whose migType is another type keep the
+ *   caller's values; a body inside migStopAt gets zeros and migType No.
+ * Requires a nebula except for GRAVITY. */
+int sol_accel_term(sol_ctx* ctx, int32_t term, double t, const double* y, double* out);
+
+enum sol_helper {
+  SOL_HELPER_TYPE_I_MIGRATION_TIME = 0,   /* TypeIMigrationTime(C, O, ar, er, h), Acceleration.cpp:766-777 */
+  SOL_HELPER_TYPE_I_ECC_DAMPING_TIME = 1, /* TypeIEccentricityDampingTime(C, O, ar, er, h), :779-789 */
+  SOL_HELPER_TAU_NU = 2                   /* TauNu(r, O), :831-849 */
+};
+/* The scalar helpers of Acceleration with the context's nebula; args holds
+ * the reference arguments in order (5, or 2 for TauNu). */
+int sol_migration_helper(sol_ctx* ctx, int32_t which, const double* args, double* out);
+
+/* RungeKuttaFehlberg78::GetErrorMax(n, yerr, yscale) = max |yerr/yscale| /
+ * epsilon (RungeKuttaFehlberg78.cpp:252-262) or DormandPrince::GetErrorMax(n,
+ * yerr) = max |yerr| (DormandPrince.cpp:493-503) on host arrays of n
+ * entries (n <= 6N with a context; ctx may be NULL, as the reference's
+ * GetErrorMax has no Acceleration: the current device is used); NaN entries
+ * never become the maximum, as in the reference's comparison.  yscale and
+ * epsilon are ignored for DormandPrince. */
+int sol_error_max(sol_ctx* ctx, int32_t integrator, int32_t n, const double* yerr, const double* yscale,
+                  double epsilon, double* out);
+
+/* One attempt of RungeKuttaFehlberg78::Step (:147-250), RungeKutta4::Step
+ * (RungeKutta4.cpp:58-129) or DormandPrince::Step2 (DormandPrince.cpp:246-491)
+ * from host y0 at (t, h), with f0 = BodyData::accel given by the caller and,
+ * for RKF78, BodyData::yscale (NULL: the Driver's yscale from y0, f0 and h).
+ * The stage evaluations use the context's evaluate flags (sol_set_eval_flags).
+ * Writes y[6N], error[6N] (RKF78 and DP; may be NULL) and error_max (the
+ * integrator's GetErrorMax; 0 for RK4).  The context's resident state
+ * becomes y0. */
+int sol_integrator_attempt(sol_ctx* ctx, int32_t integrator, double t, double h, const double* y0,
+                           const double* f0, const double* yscale, double* y, double* error, double* error_max);
+
+/* What the last driver call or attempt leaves in BodyData: accel (f0 of the
+ * step), yscale and error (of the last attempt), 6N entries each; NULL skips. */
+int sol_get_driver_vectors(sol_ctx* ctx, double* accel, double* yscale, double* error);
+/* Acceleration's persistent side buffers accelGasDrag[3 (superPlanetesimal +
+ * planetesimal)], accelMigrationTypeI[3 (rockyPlanet + protoPlanet)] and
+ * accelMigrationTypeII[3 giantPlanet] (Acceleration.cpp:176-243); NULL skips. */
+int sol_get_side_buffers(sol_ctx* ctx, double* drag, double* mig1, double* mig2);
+
 /* ---- events: predicates of Simulator::CheckEvent (Solaris/Simulator.cpp:626-645,
  * :690-729) evaluated on the device from the last force evaluation. ------ */
 int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double collision_factor,

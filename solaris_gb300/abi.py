@@ -39,6 +39,8 @@ DORMAND_PRINCE, RUNGE_KUTTA4, RUNGE_KUTTA56, RUNGE_KUTTA_FEHLBERG78 = 0, 1, 2, 3
 PRECISION_FP64, PRECISION_SPLIT, PRECISION_SPLIT_FF = 0, 1, 2
 # evaluate flags
 EVAL_GAS_DRAG, EVAL_TYPE_I, EVAL_TYPE_II, EVAL_ALL = 1, 2, 4, 7
+TERM_GRAVITY, TERM_GAS_DRAG, TERM_TYPE_I, TERM_TYPE_II = 0, 1, 2, 3
+HELPER_TYPE_I_MIGRATION_TIME, HELPER_TYPE_I_ECC_DAMPING_TIME, HELPER_TAU_NU = 0, 1, 2
 # quirks
 QUIRK_INT_ABS, QUIRK_BC_TAU_NU = 1, 2
 QUIRKS_REFERENCE = QUIRK_INT_ABS | QUIRK_BC_TAU_NU
@@ -192,6 +194,13 @@ def _declare(lib):
         "sol_ensemble_configure": (C.c_int, [P, C.c_int32, C.c_int32]),
         "sol_ensemble_autotune": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_double)]),
+        "sol_accel_term": (C.c_int, [P, C.c_int32, C.c_double, _PF64, _PF64]),
+        "sol_migration_helper": (C.c_int, [P, C.c_int32, _PF64, _PF64]),
+        "sol_error_max": (C.c_int, [P, C.c_int32, C.c_int32, _PF64, _PF64, C.c_double, _PF64]),
+        "sol_integrator_attempt": (C.c_int, [P, C.c_int32, C.c_double, C.c_double, _PF64, _PF64, _PF64, _PF64,
+                                             _PF64, _PF64]),
+        "sol_get_driver_vectors": (C.c_int, [P, _PF64, _PF64, _PF64]),
+        "sol_get_side_buffers": (C.c_int, [P, _PF64, _PF64, _PF64]),
         "sol_gravity_noalloc": (C.c_int, [C.POINTER(SolNBodies), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     }
@@ -212,7 +221,9 @@ def exported_names():
         "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc",
         "sol_ensemble_create", "sol_ensemble_destroy", "sol_ensemble_set_precision", "sol_ensemble_set_tolerance",
         "sol_ensemble_set_state", "sol_ensemble_get_state", "sol_ensemble_advance", "sol_ensemble_configure",
-        "sol_ensemble_autotune", "sol_adjoint_forward", "sol_adjoint_backward", "sol_set_masses"]
+        "sol_ensemble_autotune", "sol_adjoint_forward", "sol_adjoint_backward", "sol_set_masses",
+        "sol_accel_term", "sol_migration_helper", "sol_error_max", "sol_integrator_attempt",
+        "sol_get_driver_vectors", "sol_get_side_buffers"]
 
 
 def load_library(path: str | None = None):

@@ -326,12 +326,13 @@ inline TimeSpec stage_time(sol_ctx* c, double coef) {
 // One RKF78 attempt (RungeKuttaFehlberg78::Step, :147-250): 12 stages, the
 // final sum, the error estimate and its norm.  The time of every stage is the
 // step's start time (:168, :173-234).
-int rkf78_attempt(sol_ctx* c, const double* y0, double* y, double* err) {
+// fl: the evaluate flags of the stage evaluations; the Driver leaves only the
+// gas drag on (migration only at its first evaluation, :94-95).
+int rkf78_attempt(sol_ctx* c, const double* y0, double* y, double* err, uint32_t fl = SOL_EVAL_GAS_DRAG) {
   const Rkf78Stage* st = rkf78_stages();
   double* fk[13];
   fk[0] = c->d_accel;
   for (int k = 1; k < 13; ++k) fk[k] = c->d_fk[k];
-  const uint32_t fl = SOL_EVAL_GAS_DRAG;  // migration only at the Driver's first evaluation (:94-95)
   for (int r = 1; r <= 12; ++r) {
     StageArgs s;
     memset(&s, 0, sizeof(s));
@@ -395,11 +396,9 @@ int rkf78_driver_step(sol_ctx* c) {
   return SOL_OK;
 }
 
-int rk4_driver_step(sol_ctx* c) {
-  // RungeKutta4::Driver / Step (RungeKutta4.cpp:20-129)
-  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl, 0, 0);
-  SOL_LAUNCHED();
-  RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
+// RungeKutta4::Step (RungeKutta4.cpp:58-129): three stages from f0 = d_accel
+// and the final sum into y.
+int rk4_attempt(sol_ctx* c, const double* y0, double* y, uint32_t fl = SOL_EVAL_GAS_DRAG) {
   const double a21 = 1.0 / 2.0, a32 = 1.0 / 2.0, a43 = 1.0;
   const double b1 = 1.0 / 6.0, b2 = 1.0 / 3.0, b3 = 1.0 / 3.0, b4 = 1.0 / 6.0;
   const double c2 = 1.0 / 2.0, c3 = 1.0 / 2.0, c4 = 1.0;
@@ -407,16 +406,16 @@ int rk4_driver_step(sol_ctx* c) {
   memset(&s, 0, sizeof(s));
   s.f[0] = c->d_accel;
   s.a[0] = a21;
-  RET(launch_stage(c, 1, s, c->d_y0, c->d_ytmp));
-  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[1], stage_time(c, c2), SOL_EVAL_GAS_DRAG));
+  RET(launch_stage(c, 1, s, y0, c->d_ytmp));
+  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[1], stage_time(c, c2), fl));
   s.f[0] = c->d_fk[1];
   s.a[0] = a32;
-  RET(launch_stage(c, 1, s, c->d_y0, c->d_ytmp));
-  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[2], stage_time(c, c3), SOL_EVAL_GAS_DRAG));
+  RET(launch_stage(c, 1, s, y0, c->d_ytmp));
+  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[2], stage_time(c, c3), fl));
   s.f[0] = c->d_fk[2];
   s.a[0] = a43;
-  RET(launch_stage(c, 1, s, c->d_y0, c->d_ytmp));
-  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[3], stage_time(c, c4), SOL_EVAL_GAS_DRAG));
+  RET(launch_stage(c, 1, s, y0, c->d_ytmp));
+  RET(sol_force_launch(c, c->d_ytmp, c->d_fk[3], stage_time(c, c4), fl));
   StageArgs fs;
   memset(&fs, 0, sizeof(fs));
   fs.f[0] = c->d_accel;
@@ -427,7 +426,15 @@ int rk4_driver_step(sol_ctx* c) {
   fs.a[1] = b2;
   fs.a[2] = b3;
   fs.a[3] = b4;
-  RET(launch_stage(c, 4, fs, c->d_y0, c->d_y));
+  return launch_stage(c, 4, fs, y0, y);
+}
+
+int rk4_driver_step(sol_ctx* c) {
+  // RungeKutta4::Driver (RungeKutta4.cpp:20-57)
+  k_begin_step<<<1, 1, 0, c->stream>>>(c->d_ctrl, 0, 0);
+  SOL_LAUNCHED();
+  RET(sol_force_launch(c, c->d_y0, c->d_accel, stage_time(c, 0.0), SOL_EVAL_ALL));
+  RET(rk4_attempt(c, c->d_y0, c->d_y));
   k_control_rk4<<<1, 1, 0, c->stream>>>(c->d_ctrl);
   SOL_LAUNCHED();
   SOL_CUDA(cudaMemcpyAsync(c->d_y0, c->d_y, sizeof(double) * c->nv, cudaMemcpyDeviceToDevice, c->stream));
@@ -490,7 +497,7 @@ int launch_dp_stage(sol_ctx* c, int k, const DpStageArgs& s) {
 }
 
 // One DormandPrince::Step2 attempt: 8 stages, the final sums, the error and its norm.
-int dp_attempt(sol_ctx* c) {
+int dp_attempt(sol_ctx* c, uint32_t fl = SOL_EVAL_GAS_DRAG) {
   const DpTab& T = dp_tab();
   double* f[9];
   f[0] = c->d_accel;
@@ -516,7 +523,7 @@ int dp_attempt(sol_ctx* c) {
       }
       s.ck = T.c[k];
       RET(launch_dp_stage(c, nt, s));
-      RET(sol_force_launch(c, c->d_ytmp, f[k], stage_time(c, T.c[k]), SOL_EVAL_GAS_DRAG));
+      RET(sol_force_launch(c, c->d_ytmp, f[k], stage_time(c, T.c[k]), fl));
     }
     DpFinalArgs fa;
     for (int k = 0; k < 9; ++k) {
@@ -692,6 +699,37 @@ int sol_rkf78_single_attempt(sol_ctx* c, double t, double h, const double* d_y0,
 }
 
 int sol_integrate_partials_needed(int nv) { return grid_for(nv); }
+
+// One attempt from the resident d_y0 with f0 = d_accel (and, for RKF78, the
+// yscale in d_yscale; k_yscale fills it from f0 when compute_yscale is set):
+// RungeKuttaFehlberg78::Step, RungeKutta4::Step or DormandPrince::Step2 with
+// the given evaluate flags, into d_y and d_err; the error norm of RKF78 / DP
+// lands in the control block.  t and h come from the host.
+int sol_attempt_launch(sol_ctx* c, int integrator, double t, double h, uint32_t flags, int compute_yscale) {
+  sol_ctrl hc;
+  memset(&hc, 0, sizeof(hc));
+  hc.t = t;
+  hc.h = h;
+  hc.h_next = h;
+  hc.eps = c->eps;
+  SOL_CUDA(cudaMemcpyAsync(c->d_ctrl, &hc, sizeof(hc), cudaMemcpyHostToDevice, c->stream));
+  if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78) {
+    if (compute_yscale) {
+      k_yscale<<<grid_for(c->nv), kBlock, 0, c->stream>>>(c->nv, c->d_y0, c->d_accel, c->d_yscale, c->d_ctrl);
+      SOL_LAUNCHED();
+    }
+    RET(rkf78_attempt(c, c->d_y0, c->d_y, c->d_err, flags));
+  } else if (integrator == SOL_RUNGE_KUTTA4) {
+    RET(rk4_attempt(c, c->d_y0, c->d_y, flags));
+  } else if (integrator == SOL_DORMAND_PRINCE) {
+    RET(dp_attempt(c, flags));
+  } else {
+    sol_set_error("unknown integrator %d", integrator);
+    return SOL_ERR_ARG;
+  }
+  RET(read_ctrl(c));
+  return ctrl_status(c);
+}
 
 // One fixed-h RungeKuttaFehlberg78::Step without the error estimate: the first
 // evaluation at y0, 12 stages and the 7th-order result into y.  Stage inputs go

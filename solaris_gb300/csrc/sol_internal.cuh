@@ -332,6 +332,34 @@ __device__ __forceinline__ void sol_orbital_a_e(double mu, const double* p, int 
   *a = -mu / (2.0 * h);
 }
 
+// Acceleration::TypeIMigrationTime (Acceleration.cpp:766-777)
+__device__ __forceinline__ double sol_type1_migration_time(const GasDev& g, double C, double O, double ar, double er,
+                                                           double h) {
+  double Cm = 2.0 / (2.7 + 1.1 * g.abs_rho_index) / O;
+  double er1 = er / (1.3 * h);
+  double er2 = er / (1.1 * h);
+  double frac = (1.0 + er1 * er1 * er1 * er1 * er1) / (1.0 - er2 * er2 * er2 * er2);
+  return Cm * C * (ar * ar) * frac;
+}
+
+// Acceleration::TypeIEccentricityDampingTime (Acceleration.cpp:779-789)
+__device__ __forceinline__ double sol_type1_ecc_damping_time(double C, double O, double ar, double er, double h) {
+  double Ce = 0.1 / (0.78 * O);
+  double q = er / h;
+  double fr = 1.0 + 0.25 * (q * q * q);
+  return Ce * C * (ar * ar * ar * ar) * fr;
+}
+
+// Acceleration::TauNu (Acceleration.cpp:831-849)
+__device__ __forceinline__ double sol_tau_nu(const GasDev& g, double r, double O) {
+  double h = sol_pl(g.sh_c, g.sh_i, r);
+  if (g.tau_i == 2) {
+    double q = r / h;
+    return g.tau_c * (q * q) / (g.alpha * O);
+  }
+  return g.tau_c * pow(r / h, g.tau_i) / (g.alpha * O);
+}
+
 // MigrationTypeIAC body (Acceleration.cpp:435-481); returns false when the body
 // stops migrating (r <= migStopAt), which the caller records.
 __device__ __forceinline__ bool sol_migration_type1(const GasDev& g, double factor, double m0, double m,
@@ -352,17 +380,10 @@ __device__ __forceinline__ bool sol_migration_type1(const GasDev& g, double fact
   double er = e * r;
   double tm = 0.0;
   if (e < 1.1 * h / r) {
-    double Cm = 2.0 / (2.7 + 1.1 * g.abs_rho_index) / O;  // TypeIMigrationTime, :766-777
-    double er1 = er / (1.3 * h);
-    double er2 = er / (1.1 * h);
-    double frac = (1.0 + er1 * er1 * er1 * er1 * er1) / (1.0 - er2 * er2 * er2 * er2);
-    tm = Cm * C * (ar * ar) * frac;
+    tm = sol_type1_migration_time(g, C, O, ar, er, h);
     tm = 1.0 / tm;
   }
-  double Ce = 0.1 / (0.78 * O);  // TypeIEccentricityDampingTime, :779-789
-  double q = er / h;
-  double fr = 1.0 + 0.25 * (q * q * q);
-  double te = Ce * C * (ar * ar * ar * ar) * fr;
+  double te = sol_type1_ecc_damping_time(C, O, ar, er, h);
   double ti = te;
   double vr = yi[0] * yi[3] + yi[1] * yi[4] + yi[2] * yi[5];
   te = 2.0 * vr / (r2 * te);
@@ -385,15 +406,7 @@ __device__ __forceinline__ bool sol_migration_type2(const GasDev& g, double fact
   double a, e;
   sol_orbital_a_e(SOL_GAUSS2 * (m0 + m), yi, g.quirks, &a, &e);
   double O = SOL_GAUSS * sqrt((m0 + m) / (a * a * a));
-  // TauNu (:831-849)
-  double h = sol_pl(g.sh_c, g.sh_i, r);
-  double tau;
-  if (g.tau_i == 2) {
-    double q = r / h;
-    tau = g.tau_c * (q * q) / (g.alpha * O);
-  } else {
-    tau = g.tau_c * pow(r / h, g.tau_i) / (g.alpha * O);
-  }
+  double tau = sol_tau_nu(g, r, O);
   double c0 = (g.barycentric && (g.quirks & SOL_QUIRK_BC_TAU_NU)) ? tau : 1.0 / tau;
   double vr = yi[3] * yi[0] + yi[4] * yi[1] + yi[5] * yi[2];
   double c1 = vr / r2;
