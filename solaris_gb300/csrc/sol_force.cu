@@ -401,6 +401,164 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
   out[5] = a[2];
 }
 
+// ---- FP64 GravityAC for systems of up to a few ten thousand bodies ----------
+// One thread per sink leaves most SMs idle when the sinks number a few
+// thousand or fewer.  Here a CTA takes kFewSinks sinks: producer warps compute
+// the pair terms of a tile of kFewTile sources for all of them in parallel
+// (the reference's arithmetic, Acceleration.cpp:294-317) into a
+// double-buffered shared tile, while warp 0 adds the previous tile's terms
+// per sink and component in ascending source order.  The sums are the
+// reference's sequential sums, so the result is bit-identical to it and to
+// k_gravity_ac, with kFewSinks x kFewTile-way parallelism per CTA.  Measured
+// on the GB300 it matches or beats k_gravity_ac from 1,033 to 65,536 bodies
+// (9.0 / 13.7 G pairs/s at 1,033 / 32,768 all-massive bodies), so it serves
+// every system whose sinks see at least one tile of sources.
+constexpr int kFewSinks = 4;
+constexpr int kFewProducers = 7;                      // warps 1..7
+constexpr int kFewTile = kFewProducers * 32;          // 224 sources per round
+constexpr int kFewTerms = kFewSinks * 3;              // (sink, component) lanes of warp 0
+
+__global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const double* __restrict__ y,
+                                                        double* __restrict__ dydt, TimeSpec ts, uint32_t flags) {
+  // the nearest-neighbour candidates reuse the term tiles once the last one
+  // has been added
+  static_assert(sizeof(long long) * kFewSinks * kFewTile + sizeof(int) * kFewSinks * kFewTile <=
+                    sizeof(double) * 2 * kFewTile * kFewTerms,
+                "candidate arrays must fit in the term tiles");
+  __shared__ __align__(16) double terms[2][kFewTile][kFewTerms];
+  long long(*nn_r)[kFewTile] = reinterpret_cast<long long(*)[kFewTile]>(&terms[0][0][0]);
+  int(*nn_j)[kFewTile] = reinterpret_cast<int(*)[kFewTile]>(&terms[0][0][0] + kFewSinks * kFewTile);
+  __shared__ double sink_pos[kFewSinks][3];
+  __shared__ int sink_ns[kFewSinks];
+  __shared__ double acc[kFewTerms];
+  const Classes& c = fc.cls;
+  const int n = c.n;
+  const int i0 = blockIdx.x * kFewSinks;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < kFewSinks) {
+    const int i = i0 + threadIdx.x;
+    const bool live = i < n && i >= 1;
+    sink_ns[threadIdx.x] = live ? ((fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm) : 0;
+    for (int k = 0; k < 3; ++k) sink_pos[threadIdx.x][k] = i < n ? y[6 * i + k] : 0.0;
+  }
+  __syncthreads();
+  int ns_cta = 0;
+  for (int s = 0; s < kFewSinks; ++s) ns_cta = max(ns_cta, sink_ns[s]);
+  const int rounds = (ns_cta + kFewTile - 1) / kFewTile;
+  const double* src = fc.src;
+  const int np = fc.npad;
+
+  // producer state: the first minimum over this thread's columns, per sink
+  long long rminb[kFewSinks];
+  int nn[kFewSinks];
+  for (int s = 0; s < kFewSinks; ++s) {
+    rminb[s] = __double_as_longlong(1.0e10);
+    nn[s] = -1;
+  }
+  // accumulator state (warp 0, lanes < kFewTerms): lane = component * kFewSinks + sink
+  const int a_s = lane % kFewSinks, a_c = lane / kFewSinks;
+  const int a_i = i0 + a_s;
+  const int a_ns = (lane < kFewTerms) ? sink_ns[a_s] : 0;
+  double a_sum = 0.0;
+
+  // round r: producers fill buffer r & 1 with sources [r * kFewTile, ...);
+  // warp 0 adds buffer (r - 1) & 1
+  for (int r = 0; r <= rounds; ++r) {
+    if (warp > 0 && r < rounds) {
+      const int p = threadIdx.x - 32;
+      const int j = r * kFewTile + p;
+      if (j < ns_cta) {
+        const double xj = src[SX * np + j], yj = src[SY * np + j], zj = src[SZ * np + j];
+        const double gm = src[SGM * np + j], px = src[SPX * np + j], py = src[SPY * np + j],
+                     pz = src[SPZ * np + j];
+        double* out = &terms[r & 1][p][0];
+#pragma unroll
+        for (int s = 0; s < kFewSinks; ++s) {
+          const int i = i0 + s;
+          if (j >= 1 && j < sink_ns[s] && j != i) {
+            const double xij = xj - sink_pos[s][0];
+            const double yij = yj - sink_pos[s][1];
+            const double zij = zj - sink_pos[s][2];
+            const double rij2 = xij * xij + yij * yij + zij * zij;
+            const double rij = __dsqrt_rn(rij2);
+            const double rijm3 = __ddiv_rn(1.0, rij2 * rij);
+            const long long rb = __double_as_longlong(rij);
+            if (rb < rminb[s]) {
+              rminb[s] = rb;
+              nn[s] = j;
+            }
+            out[0 * kFewSinks + s] = gm * (xij * rijm3 - px);
+            out[1 * kFewSinks + s] = gm * (yij * rijm3 - py);
+            out[2 * kFewSinks + s] = gm * (zij * rijm3 - pz);
+          }
+        }
+      }
+    } else if (warp == 0 && r > 0 && lane < kFewTerms) {
+      const int rr = r - 1;
+      const int j0 = rr * kFewTile;
+      const int pmax = min(kFewTile, a_ns - j0);
+      for (int p = 0; p < pmax; ++p) {
+        const int j = j0 + p;
+        if (j >= 1 && j != a_i) a_sum += terms[rr & 1][p][lane];
+      }
+    }
+    __syncthreads();
+  }
+  // nearest neighbour: the smallest distance, ties to the lowest index -- the
+  // reference's first strict minimum in ascending order
+  if (warp > 0) {
+    const int p = threadIdx.x - 32;
+    for (int s = 0; s < kFewSinks; ++s) {
+      nn_r[s][p] = rminb[s];
+      nn_j[s][p] = nn[s];
+    }
+  }
+  if (warp == 0 && lane < kFewTerms) acc[lane] = a_sum;
+  __syncthreads();
+  if (threadIdx.x >= kFewSinks) return;
+  const int s = threadIdx.x;
+  const int i = i0 + s;
+  if (i >= n) return;
+  double* out = dydt + 6 * i;
+  if (i == 0) {  // GravityAC :253-254, :266
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    fc.nn_idx[0] = -1;
+    fc.nn_dist[0] = 0.0;
+    return;
+  }
+  long long best = __double_as_longlong(1.0e10);
+  int bj = -1;
+  const int pmax = min(kFewTile, ns_cta);  // producers beyond the source count hold no candidate
+  for (int p = 0; p < pmax; ++p) {
+    const long long rb = nn_r[s][p];
+    const int jb = nn_j[s][p];
+    if (jb >= 0 && (rb < best || (rb == best && jb < bj))) {
+      best = rb;
+      bj = jb;
+    }
+  }
+  const double* yv = y + 6 * i;
+  const double xi = sink_pos[s][0], yi = sink_pos[s][1], zi = sink_pos[s][2];
+  const double mu = SOL_GAUSS2 * (fc.mass[0] + fc.mass[i]);
+  const double rm3i = fc.rm3[i];
+  double a[3];
+  a[0] = -mu * rm3i * xi;  // Kepler term first (:281-283)
+  a[1] = -mu * rm3i * yi;
+  a[2] = -mu * rm3i * zi;
+  a[0] += acc[0 * kFewSinks + s];
+  a[1] += acc[1 * kFewSinks + s];
+  a[2] += acc[2 * kFewSinks + s];
+  fc.nn_idx[i] = bj;
+  fc.nn_dist[i] = bj >= 0 ? __longlong_as_double(best) : 0.0;
+  add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
+  out[0] = yv[3];
+  out[1] = yv[4];
+  out[2] = yv[5];
+  out[3] = a[0];
+  out[4] = a[1];
+  out[5] = a[2];
+}
+
 // GravityBC_SelfInteracting / _NonSelfInteracting (Acceleration.cpp:541-634):
 // massive sinks and non-massive sinks both sum over massive sources in
 // descending order, scale by G at the end; no rm3.
@@ -656,6 +814,165 @@ __global__ void k_combine(ForceCtx fc, const double* __restrict__ y, double* __r
   out[5] = a[2];
 }
 
+// ---- split forms for systems of up to kFewSplitMax bodies --------------------
+// The 2-D split kernel has ceil(N / 128) x ceil(N / 4096) work units, too few
+// to fill the GPU below ~16,000 bodies.  Here one warp takes one sink and its
+// lanes split the sources (lane l takes l, l + 32, ...): each lane
+// accumulates its share in the split arithmetic (SPLIT: FP64 FMA; SPLIT_FF:
+// float-float folded into compensated FP64 every kFoldRounds of its
+// sources), then the warp adds the 32 partials in a fixed shuffle tree with
+// compensation (deterministic) and lane 0 finishes as k_combine does.  Every
+// FP64 instruction runs on full warps: on the GB300 the FP64 pipe is scarce
+// and is charged per warp instruction.
+constexpr int kFewSplitWarps = 8;
+constexpr int kFewSplitMax = 16384;
+constexpr int kFoldRounds = 64;
+
+__device__ __forceinline__ void warp_two_sum(double& s, double& c) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const double so = __shfl_down_sync(0xffffffffu, s, off);
+    const double co = __shfl_down_sync(0xffffffffu, c, off);
+    two_sum(s, c, so);
+    c += co;
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kFewSplitWarps * 32) k_pairs_few(ForceCtx fc, const double* __restrict__ y,
+                                                                   double* __restrict__ dydt, TimeSpec ts,
+                                                                   uint32_t flags) {
+  const Classes& c = fc.cls;
+  const int n = c.n;
+  const int np = fc.npad;
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kFewSplitWarps + (threadIdx.x >> 5);
+  if (i >= n) return;  // whole warps leave together
+  const int ns = (i >= 1) ? ((fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm) : 0;
+  const double xi = y[6 * i + 0], yi = y[6 * i + 1], zi = y[6 * i + 2];
+  const double* sx = fc.src + (size_t)SX * np;
+  const double* sy = fc.src + (size_t)SY * np;
+  const double* sz = fc.src + (size_t)SZ * np;
+  double ax = 0.0, ay = 0.0, az = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+  double r2best = 1.0e300;  // this lane's first minimum of r^2 (ascending j)
+  int nn = -1;
+  if constexpr (MODE == SOL_PRECISION_SPLIT) {
+    const double* sg = fc.src + (size_t)SGM * np;
+    long long r2b = __double_as_longlong(1.0e20);
+#pragma unroll 4
+    for (int j = lane; j < ns; j += 32) {
+      const double dx = sx[j] - xi, dy = sy[j] - yi, dz = sz[j] - zi;
+      const double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, dz * dz));
+      int hi = __double2hiint(r2);
+      hi = min(max(hi, 0x38100000), 0x47EFFFFF);
+      const float f = __int_as_float((hi - 0x38000000) << 3);
+      const int fb = __float_as_int(rsqrtf(f));
+      const double y0 = __hiloint2double((fb >> 3) + 0x38000000, fb << 29);
+      const double u = y0 * y0;
+      const double e = __fma_rn(-r2, u, 1.0);
+      const double y3 = u * y0;
+      const double corr = __fma_rn(e, __fma_rn(e, 1.875, 1.5), 1.0);
+      const double gm = (j >= 1 && j != i) ? sg[j] : 0.0;  // the sink itself and the central body: 0
+      const double sc = (gm * y3) * corr;
+      ax = __fma_rn(sc, dx, ax);
+      ay = __fma_rn(sc, dy, ay);
+      az = __fma_rn(sc, dz, az);
+      const long long rb = __double_as_longlong(r2);
+      const bool better = (rb < r2b) & (j >= 1) & (j != i);
+      r2b = better ? rb : r2b;
+      nn = better ? j : nn;
+    }
+    if (nn >= 0) r2best = __longlong_as_double(r2b);
+  } else {
+    const float2* sg = reinterpret_cast<const float2*>(fc.src + (size_t)SGF * np);
+    FFAcc A;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) A.h[k] = A.l[k] = 0.0f;
+    double fx = 0.0, fy = 0.0, fz = 0.0;  // the FP64 branch of very close pairs
+    float mh = 1.0e20f, ml = 0.0f;
+    int round = 0;
+#pragma unroll 2
+    for (int j = lane; j < ns; j += 32) {
+      const float2 g = (j >= 1) ? sg[j] : make_float2(0.0f, 0.0f);  // the sink itself contributes 0 * d = 0
+      float r2h, r2l;
+      ff_pair_accumulate(sx[j] - xi, sy[j] - yi, sz[j] - zi, g, A, fx, fy, fz, r2h, r2l);
+      const bool better = ((r2h < mh) | ((r2h == mh) & (r2l < ml))) & (j >= 1) & (j != i);
+      mh = better ? r2h : mh;
+      ml = better ? r2l : ml;
+      nn = better ? j : nn;
+      if (++round == kFoldRounds) {
+        round = 0;
+        two_sum(ax, cx, (double)A.h[0] + (double)A.l[0]);
+        two_sum(ay, cy, (double)A.h[1] + (double)A.l[1]);
+        two_sum(az, cz, (double)A.h[2] + (double)A.l[2]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) A.h[k] = A.l[k] = 0.0f;
+      }
+    }
+    // the float-float remainder and the FP64 close pairs
+    two_sum(ax, cx, ((double)A.h[0] + (double)A.l[0]) + fx);
+    two_sum(ay, cy, ((double)A.h[1] + (double)A.l[1]) + fy);
+    two_sum(az, cz, ((double)A.h[2] + (double)A.l[2]) + fz);
+    if (nn >= 0) r2best = (double)mh + (double)ml;
+  }
+  warp_two_sum(ax, cx);
+  warp_two_sum(ay, cy);
+  warp_two_sum(az, cz);
+  // nearest neighbour: the smallest r^2, ties to the lower index
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const double ro = __shfl_down_sync(0xffffffffu, r2best, off);
+    const int jo = __shfl_down_sync(0xffffffffu, nn, off);
+    if (jo >= 0 && (nn < 0 || ro < r2best || (ro == r2best && jo < nn))) {
+      r2best = ro;
+      nn = jo;
+    }
+  }
+  if (lane != 0) return;
+  double* out = dydt + 6 * i;
+  if (i == 0) {
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    fc.nn_idx[0] = -1;
+    fc.nn_dist[0] = 0.0;
+    return;
+  }
+  const double* yv = y + 6 * i;
+  const double mu = SOL_GAUSS2 * (fc.mass[0] + fc.mass[i]);
+  const double rm3i = fc.rm3[i];
+  double a[3];
+  a[0] = -mu * rm3i * xi;
+  a[1] = -mu * rm3i * yi;
+  a[2] = -mu * rm3i * zi;
+  const double* S = fc.ind_sum + ((fc.type[i] <= SOL_PROTO_PLANET) ? 3 : 0);
+  const double* src = fc.src;
+  double own[3] = {0.0, 0.0, 0.0};
+  if (i < ns) {
+    const double gmi = src[SGM * np + i];
+    own[0] = gmi * src[SPX * np + i];
+    own[1] = gmi * src[SPY * np + i];
+    own[2] = gmi * src[SPZ * np + i];
+  }
+  a[0] += (ax + cx) - (S[0] - own[0]);
+  a[1] += (ay + cy) - (S[1] - own[1]);
+  a[2] += (az + cz) - (S[2] - own[2]);
+  double rij = 0.0;
+  if (nn >= 0) {
+    // the reference's rij for this j (Acceleration.cpp:301-305), bit for bit
+    const double xij = y[6 * nn + 0] - xi, yij = y[6 * nn + 1] - yi, zij = y[6 * nn + 2] - zi;
+    rij = __dsqrt_rn(xij * xij + yij * yij + zij * zij);
+    if (!(rij < 1.0e10)) nn = -1;
+  }
+  fc.nn_idx[i] = nn;
+  fc.nn_dist[i] = nn >= 0 ? rij : 0.0;
+  add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
+  out[0] = yv[3];
+  out[1] = yv[4];
+  out[2] = yv[5];
+  out[3] = a[0];
+  out[4] = a[1];
+  out[5] = a[2];
+}
+
 }  // namespace
 
 // parts: 1 = prepass (and indirect totals), 2 = pair kernel, 3 = both.
@@ -675,6 +992,22 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
   const int nb = (c->n + kSinkBlock - 1) / kSinkBlock;
   if (c->barycentric) {
     k_gravity_bc<<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
+    SOL_LAUNCHED();
+    return SOL_OK;
+  }
+  // sinks with fewer sources than one producer tile (a few massive bodies and
+  // many light ones) are cheaper with one thread per sink
+  if (!split && c->cls.nm + c->cls.n_spl >= kFewTile) {
+    k_gravity_ac_few<<<(c->n + kFewSinks - 1) / kFewSinks, 256, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
+    SOL_LAUNCHED();
+    return SOL_OK;
+  }
+  if (split && c->n <= kFewSplitMax && c->cls.nm + c->cls.n_spl >= kTile) {
+    const int grid = (c->n + kFewSplitWarps - 1) / kFewSplitWarps;
+    if (c->precision == SOL_PRECISION_SPLIT_FF)
+      k_pairs_few<SOL_PRECISION_SPLIT_FF><<<grid, kFewSplitWarps * 32, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
+    else
+      k_pairs_few<SOL_PRECISION_SPLIT><<<grid, kFewSplitWarps * 32, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
     SOL_LAUNCHED();
     return SOL_OK;
   }

@@ -117,9 +117,11 @@ def test_full_size_fp64_checksum_and_split_bound():
             assert abs(nds[i] - nd[i]) <= 1e-13 * nd[i]
 
 
-@pytest.mark.parametrize("n", [2, 3, 17, 255, 257, 1000])
+@pytest.mark.parametrize("n", [2, 3, 17, 255, 256, 257, 1000, 4097, 16384, 16385])
 def test_tails_against_oracle(n):
-    """Tile tails and tiny systems, both precisions, against the oracle."""
+    """Tile tails, tiny systems and the sizes where the kernel choice changes
+    (one thread per sink below one tile of sources; the few-sinks kernels up to
+    16,384 bodies for the split forms), every precision, against the oracle."""
     s = scenarios.config3(seed=5000 + n, n=n)
     o = oracle.Oracle(s)
     ref = o.compute(0.0, s.y0)
@@ -171,10 +173,12 @@ def test_eval_flags_and_stale_buffers():
         assert np.array_equal(ctx.mig_type(), o.mig_type())
 
 
-def test_split_ff_close_pairs_and_coincident_sink():
+@pytest.mark.parametrize("n", [64, 600])
+def test_split_ff_close_pairs_and_coincident_sink(n):
     """Float-float branch limits: a pair closer than 1e-12 AU is evaluated in
-    FP64 by the fall-back branch; the sink itself contributes exactly 0."""
-    s = scenarios.config3(seed=6001, n=64)
+    FP64 by the fall-back branch; the sink itself contributes exactly 0 (in
+    the 2-D kernel and in the few-sinks kernel)."""
+    s = scenarios.config3(seed=6001, n=n)
     y = s.y0.reshape(-1, 6).copy()
     y[10, :3] = y[9, :3] + np.array([3e-13, -2e-13, 1e-13])  # 3.7e-13 AU apart
     y[20, :3] = y[19, :3] + np.array([1e-9, 0.0, 0.0])
