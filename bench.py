@@ -193,6 +193,122 @@ def ensemble_section(local):
     return out
 
 
+def adjoint_section(local):
+    """Discrete adjoint of fixed-step RKF78 on the adjoint workload (1 star +
+    8 planets + 1,024 planetesimals typed ProtoPlanet, h = shortest period /
+    500): forward and backward milliseconds per step with a checkpoint every
+    100 steps, the backward / forward cost ratio (bound 4), FP64 and SPLIT_FF
+    forces; the oracle's forward step on one core beside it."""
+    import numpy as np
+
+    import oracle
+    from solaris_gb300 import engine, scenarios
+    s = scenarios.config5()
+    h, n_steps, every = s.h0 * 100, 1000, 100
+    out = {"workload": "1 star + 8 planets + 1,024 ProtoPlanet planetesimals, fixed-step RKF78, "
+                       "h = shortest period / 500, checkpoint every 100 steps",
+           "n_bodies": s.n, "steps": n_steps, "checkpoint_every": every,
+           "pairs_per_step": 11 * s.pair_count()}
+    rng = np.random.default_rng(1005)
+    for name, prec in (("fp64", 0), ("split_ff", 2)):
+        with engine.Context(s, device=local, precision=prec) as ctx:
+            ctx.adjoint_forward(s.y0, h, 20, 10)  # warm-up
+            t0 = time.perf_counter()
+            yf = ctx.adjoint_forward(s.y0, h, n_steps, every)
+            tf = time.perf_counter() - t0
+            target = yf.reshape(-1, 6)[:, :3] + 1e-6 * rng.standard_normal((s.n, 3))
+            g = np.zeros_like(yf).reshape(-1, 6)
+            g[:, :3] = 2.0 * (yf.reshape(-1, 6)[:, :3] - target)
+            t0 = time.perf_counter()
+            ctx.adjoint_backward(g.reshape(-1))
+            tb = time.perf_counter() - t0
+        out[name] = {"forward_ms_per_step": 1e3 * tf / n_steps, "backward_ms_per_step": 1e3 * tb / n_steps,
+                     "backward_over_forward": tb / tf,
+                     "forward_pairs_per_s": out["pairs_per_step"] * n_steps / tf,
+                     "projected_s_for_10000_steps": (tf + tb) * 10000 / n_steps}
+    o = oracle.Oracle(s)
+    k = 3
+    t0 = time.perf_counter()
+    o.rkf78_fixed(s.y0, h, k)
+    out["cpu_port_1_core"] = {"forward_ms_per_step": 1e3 * (time.perf_counter() - t0) / k, "kind": "port",
+                              "cores": 1, "sample": f"{k} fixed RKF78 steps of the oracle"}
+    return out
+
+
+def small_systems_section(local):
+    """The latency-bound configurations: 256 bodies (1 star, 2 giants, 253 test
+    particles; adaptive RKF78 eps 1e-10) and 8,193 bodies with a gas nebula
+    (1 star, 2 giants, 8,190 planetesimals with drag; eps 1e-11), FP64, each
+    driver call one CUDA graph with the attempt loop on the device; the
+    oracle on one core beside each."""
+    import oracle
+    from solaris_gb300 import abi, engine, scenarios
+    out = {}
+    for name, s, k, kc in (("config1_256_bodies", scenarios.config1(), 400, 100),
+                           ("config2_8193_bodies_gas", scenarios.config2(), 200, 20)):
+        with engine.Context(s, device=local) as ctx:
+            ctx.set_tolerance(s.epsilon)
+            ctx.set_state(s.y0)
+            tl = abi.SolTimeLine(0.0, s.h0, 0.0)
+            ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0, 0, 20, time_line=tl)
+            t0 = time.perf_counter()
+            r = ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0, 0, k, time_line=tl)
+            dt = time.perf_counter() - t0
+        acc, rej, evals = r["stats"]
+        o = oracle.Oracle(s)
+        o.set_eval_flags(abi.EVAL_ALL)
+        t0 = time.perf_counter()
+        ro = o.driver(abi.RUNGE_KUTTA_FEHLBERG78, s.y0, 0.0, s.h0, kc)
+        dtc = time.perf_counter() - t0
+        out[name] = {"steps_per_s": acc / dt, "evaluations_per_s": evals / dt,
+                     "pair_interactions_per_s": evals * s.pair_count() / dt,
+                     "body_evaluations_per_s": evals * s.n / dt, "accepted": acc, "rejected": rej,
+                     "cpu_port_1_core": {"steps_per_s": ro["stats"][0] / dtc,
+                                         "pair_interactions_per_s": ro["stats"][2] * s.pair_count() / dtc,
+                                         "kind": "port", "cores": 1, "sample": f"{kc} driver calls"}}
+    return out
+
+
+# FP64 pipe slots per state element of one RKF78 attempt's elementwise kernels:
+# stage r is a0 f0 + ... (2 K_r - 1) then y0 + h acc (2): sum over the 12
+# stages of 2 K_r + 1 = 122; the final sum 13, the error estimate 3 adds, 2
+# multiplications and a division by 840 (~5 slots) = 10, |e / yscale| a
+# division (~5) and the comparison (1) -- 151 in all.
+STAGE_FP64_SLOTS = 151
+
+
+def stage_sums_section(local, hbm_peak_gbs, fp64_peak_ops):
+    """Elementwise kernels of an RKF78 attempt (12 stage sums, final sum with
+    error estimate and scaled norm), event-timed, at the bench's 65,536 bodies
+    (vectors L2-resident) and at 1,048,576 bodies (vectors far larger than
+    L2): algorithmic bytes 8 * 6N * 93 per attempt against the HBM copy peak,
+    and FP64 pipe slots 151 * 6N against the FP64 peak.  With ~0.2 FP64
+    operations per byte against the GB300's 0.075 (505 G FP64 instructions/s
+    over 6.7 TB/s), the FP64 pipe is the bound."""
+    from solaris_gb300 import engine, scenarios
+    out = {"bound": "fp64", "bytes_per_attempt": "8 * 6N * 93", "fp64_slots_per_element": STAGE_FP64_SLOTS,
+           "hbm_peak_gbs": hbm_peak_gbs, "fp64_peak_gops": fp64_peak_ops / 1e9}
+    for n in (65536, 1048576):
+        s = scenarios.config3(n=n)
+        with engine.Context(s, device=local) as ctx:
+            ctx.set_state(s.y0)
+            ms = ctx.bench_stages(20)
+        gbs = 8 * 6 * n * 93 / (ms * 1e-3) / 1e9
+        gops = STAGE_FP64_SLOTS * 6 * n / (ms * 1e-3) / 1e9
+        out[f"n_{n}"] = {"ms_per_attempt": ms, "achieved_gbs": gbs,
+                         "frac_of_hbm_peak": gbs / hbm_peak_gbs if hbm_peak_gbs else None,
+                         "achieved_fp64_gops": gops, "frac_of_fp64_peak": gops * 1e9 / fp64_peak_ops}
+    return out
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["hbm_gbs"]), "MEASURED_PEAKS.json"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
 def main():
     args = parse()
     from solaris_gb300 import replicas
@@ -309,6 +425,12 @@ def main():
             forms[name]["max_rel_accel_err"], forms[name]["rms_rel_accel_err"] = acc[name]
     pps_head = pairs_eval / (ms_launch[head_name] * 1e-3)
     ensemble = ensemble_section(local) if not args.skip_ensemble else None
+    hbm_peak, hbm_src = measured_hbm_peak()
+    extra = {}
+    if not args.skip_ensemble:
+        extra["adjoint"] = adjoint_section(local)
+        extra["small_systems"] = small_systems_section(local)
+        extra["stage_sums"] = dict(stage_sums_section(local, hbm_peak, peak_ops), hbm_peak_source=hbm_src)
     cpu = None
     if rank == 0:
         n_sinks = 12288
@@ -341,6 +463,7 @@ def main():
         "gpu_launches": head["launches"],
         "clocks": head["clocks"],
         "ensemble": ensemble,
+        **extra,
     }
     if rank == 0:
         print(json.dumps(line))

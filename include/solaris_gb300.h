@@ -365,6 +365,11 @@ int sol_get_stream(sol_ctx* ctx, void** stream);
  * (no prepass), over `reps` launches on the context's resident state, timed
  * with CUDA events on the context's stream. */
 int sol_bench_force(sol_ctx* ctx, int32_t precision, int32_t reps, double* ms_per_launch);
+/* Average duration in milliseconds of the elementwise kernels of one RKF78
+ * attempt alone (12 stage sums, the final sum with the error estimate and its
+ * scaled norm, the norm reduction) over the context's stage vectors:
+ * 8 * 6N * 93 bytes of algorithmic HBM traffic per attempt. */
+int sol_bench_stages(sol_ctx* ctx, int32_t reps, double* ms_per_attempt);
 
 #ifdef __cplusplus
 }

@@ -181,6 +181,7 @@ def _declare(lib):
         "sol_kernel_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
         "sol_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
         "sol_bench_force": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
+        "sol_bench_stages": (C.c_int, [P, C.c_int32, C.POINTER(C.c_double)]),
         "sol_adjoint_forward": (C.c_int, [P, C.c_double, C.c_int32, C.c_int32, _PF64, _PF64]),
         "sol_adjoint_backward": (C.c_int, [P, _PF64, _PF64, _PF64]),
         "sol_set_masses": (C.c_int, [P, _PF64]),
@@ -223,7 +224,7 @@ def exported_names():
         "sol_ensemble_set_state", "sol_ensemble_get_state", "sol_ensemble_advance", "sol_ensemble_configure",
         "sol_ensemble_autotune", "sol_adjoint_forward", "sol_adjoint_backward", "sol_set_masses",
         "sol_accel_term", "sol_migration_helper", "sol_error_max", "sol_integrator_attempt",
-        "sol_get_driver_vectors", "sol_get_side_buffers"]
+        "sol_get_driver_vectors", "sol_get_side_buffers", "sol_bench_stages"]
 
 
 def load_library(path: str | None = None):

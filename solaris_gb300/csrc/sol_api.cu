@@ -12,6 +12,7 @@
 
 int sol_force_tile();
 int sol_force_part_doubles(int npad);
+int sol_force_uses_chunk_partials(const sol_ctx* c);
 int sol_force_prepass_blocks(int npad);
 int sol_integrate_partials_needed(int nv);
 int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_pe);
@@ -144,6 +145,7 @@ void free_ctx(sol_ctx* c) {
     if (c->d_fk[k]) cudaFree(c->d_fk[k]);
   for (int k = 0; k < 2; ++k) sol_graph_release(c->graphs[k]);
   sol_adjoint_free(c->adj);
+  if (c->d_persist) cudaFree(c->d_persist);
   if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -305,9 +307,9 @@ int sol_create(const sol_body_data* b, const sol_gas_component* gas, int32_t bar
   for (int q = 0; q < 13; ++q)
     if ((rc = dev_alloc(&c->d_fk[q], NV))) return fail(rc);
   c->n_partial = sol_integrate_partials_needed(NV);
-  if ((rc = dev_alloc(&c->d_partial, (size_t)c->n_partial + 16)) || (rc = dev_alloc(&c->d_ctrl, 1)) ||
-      (rc = dev_alloc(&c->d_part, (size_t)sol_force_part_doubles(c->npad))))
-    return fail(rc);
+  // d_part (chunk partials of the 2-D split kernel) is allocated when a split
+  // precision is first selected for a system that uses that kernel
+  if ((rc = dev_alloc(&c->d_partial, (size_t)c->n_partial + 16)) || (rc = dev_alloc(&c->d_ctrl, 1))) return fail(rc);
   if (cudaMallocHost((void**)&c->h_ctrl, sizeof(sol_ctrl)) != cudaSuccess ||
       cudaMallocHost((void**)&c->h_stage, sizeof(double) * NV) != cudaSuccess) {
     sol_set_error("cudaMallocHost failed");
@@ -375,6 +377,10 @@ int sol_set_precision(sol_ctx* c, int32_t p) {
   if (p != SOL_PRECISION_FP64 && p != SOL_PRECISION_SPLIT && p != SOL_PRECISION_SPLIT_FF) {
     sol_set_error("unknown precision %d", p);
     return SOL_ERR_ARG;
+  }
+  if (p != SOL_PRECISION_FP64 && !c->barycentric && !c->d_part && sol_force_uses_chunk_partials(c)) {
+    RET(set_device(c));
+    RET(dev_alloc(&c->d_part, (size_t)sol_force_part_doubles(c->npad)));
   }
   c->precision = p;
   c->fc.precision = p;
@@ -655,6 +661,13 @@ int sol_get_stream(sol_ctx* c, void** stream) {
   if (!stream) return SOL_ERR_ARG;
   *stream = (void*)c->stream;
   return SOL_OK;
+}
+
+int sol_bench_stages(sol_ctx* c, int32_t reps, double* ms_per_attempt) {
+  RET(check_ctx(c));
+  if (!ms_per_attempt || reps < 1) return SOL_ERR_ARG;
+  RET(set_device(c));
+  return sol_bench_stage_kernels(c, reps, ms_per_attempt);
 }
 
 int sol_bench_force(sol_ctx* c, int32_t precision, int32_t reps, double* ms_per_launch) {

@@ -119,66 +119,6 @@ __global__ void k_ind_reduce(ForceCtx fc) {
   }
 }
 
-// ---- epilogue: drag and migration of one sink (ComputeAstroCentric :176-243) --
-__device__ __forceinline__ void add_gas_terms(const ForceCtx& fc, int i, const double* yi, double t,
-                                              uint32_t flags, double a[3]) {
-  const GasDev& g = fc.gas;
-  if (!g.present) return;
-  const Classes& c = fc.cls;
-  const double m0 = fc.mass[0];
-  const int lower_drag = c.nm, upper_drag = c.nm + c.n_spl + c.n_pl;
-  if (i >= lower_drag && i < upper_drag) {
-    double* buf = fc.drag + 3 * (i - lower_drag);
-    if (flags & SOL_EVAL_GAS_DRAG) {
-      double d[3];
-      sol_gas_drag(g, sol_reduction_factor(g, t), m0, yi, fc.radius[i], fc.density[i], fc.cd[i],
-                   fc.gamma_stokes[i], fc.gamma_epstein[i], d);
-      buf[0] = d[0];
-      buf[1] = d[1];
-      buf[2] = d[2];
-    }
-    a[0] += buf[0];
-    a[1] += buf[1];
-    a[2] += buf[2];
-    return;
-  }
-  const int lower1 = c.n_central + c.n_giant;
-  if (fc.has_mig1 && i >= lower1 && i < c.nm) {
-    double* buf = fc.mig1 + 3 * (i - lower1);
-    if ((flags & SOL_EVAL_TYPE_I) && fc.mig_type[i] == SOL_MIGRATION_TYPE_I) {
-      double d[3];
-      if (!sol_migration_type1(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
-        fc.mig_type[i] = SOL_MIGRATION_NO;
-      buf[0] = d[0];
-      buf[1] = d[1];
-      buf[2] = d[2];
-    }
-    if (fc.mig_type[i] != SOL_MIGRATION_NO) {
-      a[0] += buf[0];
-      a[1] += buf[1];
-      a[2] += buf[2];
-    }
-    return;
-  }
-  const int lower2 = c.n_central;
-  if (fc.has_mig2 && i >= lower2 && i < c.n_central + c.n_giant) {
-    double* buf = fc.mig2 + 3 * (i - lower2);
-    if ((flags & SOL_EVAL_TYPE_II) && fc.mig_type[i] == SOL_MIGRATION_TYPE_II) {
-      double d[3];
-      if (!sol_migration_type2(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
-        fc.mig_type[i] = SOL_MIGRATION_NO;
-      buf[0] = d[0];
-      buf[1] = d[1];
-      buf[2] = d[2];
-    }
-    if (fc.mig_type[i] != SOL_MIGRATION_NO) {
-      a[0] += buf[0];
-      a[1] += buf[1];
-      a[2] += buf[2];
-    }
-  }
-}
-
 // ---- tile pipeline -----------------------------------------------------------
 template <int NARR>
 struct TileSmem {
@@ -1012,6 +952,10 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
     return SOL_OK;
   }
   if (split) {
+    if (!c->d_part) {
+      sol_set_error("split precision selected without sol_set_precision");
+      return SOL_ERR_STATE;
+    }
     const int nchunk = (c->n + kChunk - 1) / kChunk;
     dim3 grid(nb, nchunk);
     if (c->precision == SOL_PRECISION_SPLIT_FF)
@@ -1034,6 +978,11 @@ int sol_force_launch(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts,
 
 int sol_force_tile() { return kTile; }
 int sol_force_part_doubles(int npad) { return ((npad + kChunk - 1) / kChunk) * PART_SLOTS * npad; }
+// whether the split forms of this system run the 2-D kernel (and need its
+// chunk partials); the same test as the dispatch in sol_force_launch_parts
+int sol_force_uses_chunk_partials(const sol_ctx* c) {
+  return !(c->n <= kFewSplitMax && c->cls.nm + c->cls.n_spl >= kTile);
+}
 int sol_force_prepass_blocks(int npad) { return (npad + kPrepassBlock - 1) / kPrepassBlock; }
 
 // ---- caller-allocated variant ---------------------------------------------------

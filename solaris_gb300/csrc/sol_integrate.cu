@@ -649,6 +649,12 @@ int build_driver_graph(sol_ctx* c, int integrator, DriverGraph& G) {
 }  // namespace
 
 int sol_integrator_run(sol_ctx* c, int integrator, int n_steps) {
+  // few-source systems: every driver call of the sequence in one cooperative
+  // launch (falls through when the grid cannot be co-resident)
+  if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78 && c->device_loop && n_steps > 0 && sol_persist_eligible(c)) {
+    const int r = sol_persist_rkf78(c, n_steps);
+    if (r != SOL_ERR_STATE) return r;
+  }
   const int gi = integrator == SOL_RUNGE_KUTTA_FEHLBERG78 ? 0 : (integrator == SOL_DORMAND_PRINCE ? 1 : -1);
   if (gi >= 0 && c->device_loop && n_steps > 0) {
     DriverGraph& G = c->graphs[gi];
@@ -699,6 +705,72 @@ int sol_rkf78_single_attempt(sol_ctx* c, double t, double h, const double* d_y0,
 }
 
 int sol_integrate_partials_needed(int nv) { return grid_for(nv); }
+
+const Rkf78Table& sol_rkf78_table() {
+  static Rkf78Table T;
+  static bool init = false;
+  if (!init) {
+    memset(&T, 0, sizeof(T));
+    const Rkf78Stage* st = rkf78_stages();
+    for (int r = 1; r <= 12; ++r) {
+      T.k[r] = st[r].k;
+      for (int q = 0; q < st[r].k; ++q) {
+        T.idx[r][q] = st[r].idx[q];
+        T.a[r][q] = st[r].a[q];
+      }
+    }
+    init = true;
+  }
+  return T;
+}
+
+// The elementwise kernels of one RKF78 attempt alone -- 12 stage sums, the
+// fused final sum / error estimate / scaled norm and the norm reduction --
+// over the context's stage vectors, timed with CUDA events on the context's
+// stream: their HBM bytes per attempt are 8 * 6N * 93 (79 passes of the
+// stage sums, 9 of the final sum, 5 of the error norm).
+int sol_bench_stage_kernels(sol_ctx* c, int reps, double* ms_per_attempt) {
+  const Rkf78Stage* st = rkf78_stages();
+  double* fk[13];
+  fk[0] = c->d_accel;
+  for (int k = 1; k < 13; ++k) fk[k] = c->d_fk[k];
+  auto one = [&]() -> int {
+    for (int r = 1; r <= 12; ++r) {
+      StageArgs sa;
+      memset(&sa, 0, sizeof(sa));
+      for (int k = 0; k < st[r].k; ++k) {
+        sa.f[k] = fk[st[r].idx[k]];
+        sa.a[k] = st[r].a[k];
+      }
+      // each stage writes its own input vector, as the attempt's evaluations would read it
+      RET(launch_stage(c, st[r].k, sa, c->d_y0, r < 12 ? c->d_fk[r + 1] : c->d_ytmp));
+    }
+    Rkf78FinalArgs fa;
+    for (int k = 0; k < 13; ++k) fa.f[k] = fk[k];
+    const int g = grid_for(c->nv);
+    k_rkf78_final<<<g, kBlock, 0, c->stream>>>(c->nv, c->d_y0, fa, c->d_y, c->d_err, c->d_yscale, c->d_partial,
+                                              c->d_ctrl);
+    SOL_LAUNCHED();
+    k_reduce_max<<<1, kBlock, 0, c->stream>>>(c->d_partial, g, c->d_ctrl, 1);
+    SOL_LAUNCHED();
+    return SOL_OK;
+  };
+  RET(one());  // warm-up
+  cudaEvent_t e0, e1;
+  SOL_CUDA(cudaEventCreate(&e0));
+  SOL_CUDA(cudaEventCreate(&e1));
+  SOL_CUDA(cudaEventRecord(e0, c->stream));
+  int rc = SOL_OK;
+  for (int r = 0; r < reps && rc == SOL_OK; ++r) rc = one();
+  SOL_CUDA(cudaEventRecord(e1, c->stream));
+  SOL_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  SOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_attempt = ms / reps;
+  return rc;
+}
 
 // One attempt from the resident d_y0 with f0 = d_accel (and, for RKF78, the
 // yscale in d_yscale; k_yscale fills it from f0 when compute_yscale is set):

@@ -167,6 +167,7 @@ struct sol_ctx {
   long long graph_steps;   // driver calls run as graphs since the last sol_driver
   int graph_used;
   sol_adjoint_state* adj;  // checkpoints and buffers of the discrete adjoint
+  double* d_persist;       // source tables, block maxima and barrier words of the persistent driver
 };
 
 // ---- launch helpers (defined in sol_force.cu / sol_integrate.cu) --------------
@@ -178,6 +179,17 @@ int sol_rkf78_single_attempt(sol_ctx* c, double t, double h, const double* d_y0,
 int sol_events_launch(sol_ctx* c, const double* d_y0, double ej, double hc, double cf, sol_event* d_out,
                       int capacity, int* d_count);
 int sol_integrals_launch(sol_ctx* c, const double* d_y0, double* d_out16);
+int sol_bench_stage_kernels(sol_ctx* c, int reps, double* ms_per_attempt);
+// RKF78 stage sums in the reference's term order (RungeKuttaFehlberg78.cpp:169-232):
+// stage r = y0 + h * sum_q a[r][q] f[idx[r][q]], q < k[r]
+struct Rkf78Table {
+  int k[13];
+  int idx[13][9];
+  double a[13][9];
+};
+const Rkf78Table& sol_rkf78_table();
+int sol_persist_eligible(const sol_ctx* c);
+int sol_persist_rkf78(sol_ctx* c, int n_steps);
 int sol_fp64_peak_launch(int device, double* flops);
 
 // ---- PTX helpers: bulk copies (TMA engine) with mbarrier completion --------
@@ -414,4 +426,64 @@ __device__ __forceinline__ bool sol_migration_type2(const GasDev& g, double fact
   out[1] = -factor * (c0 * (0.5 * yi[4] + 50 * (c1 * yi[1])));
   out[2] = -factor * (c0 * (0.5 * yi[5] + 50 * (c1 * yi[2]) + yi[5]));
   return true;
+}
+
+// ---- epilogue: drag and migration of one sink (ComputeAstroCentric :176-243) --
+__device__ __forceinline__ void add_gas_terms(const ForceCtx& fc, int i, const double* yi, double t,
+                                              uint32_t flags, double a[3]) {
+  const GasDev& g = fc.gas;
+  if (!g.present) return;
+  const Classes& c = fc.cls;
+  const double m0 = fc.mass[0];
+  const int lower_drag = c.nm, upper_drag = c.nm + c.n_spl + c.n_pl;
+  if (i >= lower_drag && i < upper_drag) {
+    double* buf = fc.drag + 3 * (i - lower_drag);
+    if (flags & SOL_EVAL_GAS_DRAG) {
+      double d[3];
+      sol_gas_drag(g, sol_reduction_factor(g, t), m0, yi, fc.radius[i], fc.density[i], fc.cd[i],
+                   fc.gamma_stokes[i], fc.gamma_epstein[i], d);
+      buf[0] = d[0];
+      buf[1] = d[1];
+      buf[2] = d[2];
+    }
+    a[0] += buf[0];
+    a[1] += buf[1];
+    a[2] += buf[2];
+    return;
+  }
+  const int lower1 = c.n_central + c.n_giant;
+  if (fc.has_mig1 && i >= lower1 && i < c.nm) {
+    double* buf = fc.mig1 + 3 * (i - lower1);
+    if ((flags & SOL_EVAL_TYPE_I) && fc.mig_type[i] == SOL_MIGRATION_TYPE_I) {
+      double d[3];
+      if (!sol_migration_type1(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
+        fc.mig_type[i] = SOL_MIGRATION_NO;
+      buf[0] = d[0];
+      buf[1] = d[1];
+      buf[2] = d[2];
+    }
+    if (fc.mig_type[i] != SOL_MIGRATION_NO) {
+      a[0] += buf[0];
+      a[1] += buf[1];
+      a[2] += buf[2];
+    }
+    return;
+  }
+  const int lower2 = c.n_central;
+  if (fc.has_mig2 && i >= lower2 && i < c.n_central + c.n_giant) {
+    double* buf = fc.mig2 + 3 * (i - lower2);
+    if ((flags & SOL_EVAL_TYPE_II) && fc.mig_type[i] == SOL_MIGRATION_TYPE_II) {
+      double d[3];
+      if (!sol_migration_type2(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
+        fc.mig_type[i] = SOL_MIGRATION_NO;
+      buf[0] = d[0];
+      buf[1] = d[1];
+      buf[2] = d[2];
+    }
+    if (fc.mig_type[i] != SOL_MIGRATION_NO) {
+      a[0] += buf[0];
+      a[1] += buf[1];
+      a[2] += buf[2];
+    }
+  }
 }

@@ -116,6 +116,11 @@ class Context:
         abi.check(self.lib, self.lib.sol_get_stream(self.h, C.byref(v)))
         return int(v.value or 0)
 
+    def bench_stages(self, reps) -> float:
+        ms = C.c_double(0)
+        abi.check(self.lib, self.lib.sol_bench_stages(self.h, int(reps), C.byref(ms)))
+        return float(ms.value)
+
     def bench_force(self, precision, reps) -> float:
         ms = C.c_double(0)
         abi.check(self.lib, self.lib.sol_bench_force(self.h, int(precision), int(reps), C.byref(ms)))

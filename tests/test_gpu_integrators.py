@@ -193,6 +193,37 @@ def test_device_loop_matches_host_loop(integrator):
     assert out[1][3][1] > 0  # the run exercised rejected attempts
 
 
+@pytest.mark.parametrize("case", ["mixed_gas", "config2", "many_sources"])
+def test_persistent_and_graph_drivers_match_host_loop(case):
+    """Few-source systems run their RKF78 driver calls in one cooperative
+    launch (one thread per body, a grid barrier per stage); systems with more
+    sources run the CUDA-graph driver.  Either way: the bits, step counts,
+    time line, last evaluation (rm3, nearest neighbours) and migType of the
+    host-driven loop."""
+    if case == "mixed_gas":
+        s, n = scenarios.mixed_gas_system(seed=3300), 30
+    elif case == "config2":
+        s, n = scenarios.config2(n_pl=3000), 12
+    else:
+        s, n = scenarios.config3(seed=1602, n=300), 10
+        s.integrator = abi.RUNGE_KUTTA_FEHLBERG78
+    out = {}
+    for loop in (1, 0):
+        with engine.Context(s) as ctx:
+            ctx.set_tolerance(s.epsilon)
+            ctx.set_device_loop(loop)
+            ctx.set_state(s.y0)
+            r = ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0.0, s.h0, n)
+            out[loop] = (ctx.get_state(), (r["time"], r["h_next"], r["h_did"]), r["stats"], ctx.last_eval(),
+                         ctx.mig_type())
+    g, hst = out[1], out[0]
+    assert np.array_equal(bits(g[0]), bits(hst[0]))
+    assert g[1] == hst[1] and g[2] == hst[2]
+    for a, b in zip(g[3], hst[3]):
+        assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
+    assert np.array_equal(g[4], hst[4])
+
+
 def test_device_loop_reports_underflow():
     s = scenarios.config3(seed=78, n=17)
     with engine.Context(s) as ctx:
