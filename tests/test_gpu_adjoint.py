@@ -137,3 +137,77 @@ def test_backward_cost_within_four_forwards():
         ctx.adjoint_backward(g)
         tb = time.perf_counter() - t0
     assert tb <= 4.0 * tf, (tb, tf)
+
+
+def test_adjoint_full_size_directions():
+    """The full adjoint workload (1 star + 8 planets + 1,024 planetesimals,
+    h = shortest period / 500, 200 steps, target = final state + 1e-6 AU
+    noise): 16 random directions and 32 single coordinates against central
+    differences of the GPU forward at h = 1e-7, within 1e-6.
+
+    Directions are in units of each coordinate's scale (positions 1 AU,
+    velocities 1e-2 AU/day, masses the body's mass) with a standard normal
+    component per coordinate; a direction normalised over all 7,231
+    parameters moves each by ~1/85 of its scale and its derivative sinks to
+    the rounding noise of the loss difference.  Along directions that move
+    every body of this system the plain h = 1e-7 difference carries an h^2
+    truncation error of ~1e-5 (measured: 0.137, 1.4e-3, 1.3e-5 at h = 1e-5,
+    1e-6, 1e-7, while the oracle's tangent-linear model agrees with the
+    adjoint to 1.3e-14), so the h = 1e-7 difference is Richardson-extrapolated
+    with the 2h difference, (4 D(h) - D(2h)) / 3, which removes that term."""
+    s = scenarios.config5()
+    h, n_steps, every = s.h0 * 100, 200, 20
+    rng = np.random.default_rng(1005)
+    with engine.Context(s) as ctx:
+        y_final = ctx.adjoint_forward(s.y0, h, n_steps, every)
+        target = y_final.reshape(-1, 6)[:, :3] + 1e-6 * rng.standard_normal((s.n, 3))
+        _, g = _loss_grad(y_final, target)
+        dy0, dmass = ctx.adjoint_backward(g)
+
+        def loss(y0, mass):
+            ctx.set_masses(mass)
+            yf = ctx.adjoint_forward(y0, h, n_steps, every)
+            return _loss_grad(yf, target)[0]
+
+        scale = np.tile([1.0, 1.0, 1.0, 1e-2, 1e-2, 1e-2], s.n)
+        dirs = []
+        for _ in range(16):
+            v = rng.standard_normal(7 * s.n)
+            v[:6] = 0.0  # the central body's state is fixed
+            dirs.append((v[:6 * s.n] * scale, v[6 * s.n:] * s.mass))
+        for k in rng.choice(np.arange(6, 6 * s.n), 32, replace=False):
+            dy = np.zeros(6 * s.n)
+            dy[k] = scale[k]
+            dirs.append((dy, np.zeros(s.n)))
+        eps, rel = 1e-7, []
+
+        def central(e, dy, dm):
+            return (loss(s.y0 + e * dy, s.mass + e * dm) - loss(s.y0 - e * dy, s.mass - e * dm)) / (2 * e)
+
+        for dy, dm in dirs:
+            fd = (4.0 * central(eps, dy, dm) - central(2 * eps, dy, dm)) / 3.0
+            adj = float(dy0 @ dy + dmass @ dm)
+            rel.append((abs(adj - fd) / max(abs(fd), 1e-30), adj, fd))
+        ctx.set_masses(s.mass)
+    print("relative differences to central differences:", " ".join(f"{r[0]:.1e}" for r in rel))
+    bad = [r for r in rel if r[0] > GRAD_RTOL]
+    assert not bad, bad
+
+
+def test_adjoint_full_size_against_tangent_linear_model():
+    """Two random directions of the full adjoint workload (20 steps) against
+    the oracle's FP64 tangent-linear integration."""
+    s = scenarios.config5()
+    h, n_steps, every = s.h0 * 100, 20, 5
+    rng = np.random.default_rng(77)
+    with engine.Context(s) as ctx:
+        y_final = ctx.adjoint_forward(s.y0, h, n_steps, every)
+        target = y_final.reshape(-1, 6)[:, :3] + 1e-6 * rng.standard_normal((s.n, 3))
+        _, g = _loss_grad(y_final, target)
+        dy0, dmass = ctx.adjoint_backward(g)
+    o = oracle.Oracle(s)
+    for dy, dm in _directions(s, 2, rng):
+        _, dy_final = o.rkf78_fixed(s.y0, h, n_steps, dy, dm)
+        tlm = float(g @ dy_final)
+        adj = float(dy0 @ dy + dmass @ dm)
+        assert abs(adj - tlm) <= GRAD_RTOL * abs(tlm), (adj, tlm)
