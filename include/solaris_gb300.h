@@ -298,6 +298,45 @@ int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double c
 /* ---- diagnostics: Calculate::Integrals (Solaris/Calculate.cpp:43-62). --- */
 int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
 
+/* ---- output files: BinaryFileAdapter (Solaris/BinaryFileAdapter.cpp:107-219)
+ * Phases: per record double time, int32 n, then per body int32 id and the 6
+ * doubles of y0 (binary), or the reference's text layout (setw(15)
+ * setprecision(10) time, setw(8) n, per body setw(8) id and setw(15)
+ * setprecision(6) values, end of line).  Integrals: a length-prefixed header
+ * at the start of the file, then per record int32 (n + 1), double time and
+ * the 16 doubles of Calculate::Integrals.  Records are appended. ----------- */
+typedef struct sol_output sol_output;
+/* Either path may be NULL (that file is not written).  An integrals file
+ * gets the header when it is empty at open. */
+int sol_output_open(sol_ctx* ctx, const char* phases_path, const char* integrals_path, int32_t text,
+                    sol_output** out);
+/* Appends the context's resident state (Simulator: SavePhases(time, n, y0, id)).
+ * Costs the compute stream one device copy; the host copy and the write run
+ * on a copy stream and a writer thread while the integration continues. */
+int sol_output_save_phases(sol_output* out, double time);
+/* Calculate::Integrals of the resident state (O(N^2) potential on the device)
+ * and SaveIntegrals(time, 16, integrals). */
+int sol_output_save_integrals(sol_output* out, double time);
+int sol_output_flush(sol_output* out); /* every queued record on disk */
+int sol_output_close(sol_output* out);
+/* The records themselves, host only (length = bytes; buf NULL asks for it). */
+int sol_format_phases_record(double time, int32_t n, const double* y, const int32_t* id, int32_t text, char* buf,
+                             int64_t capacity, int64_t* length);
+int sol_format_integrals_record(double time, int32_t n, const double* integrals, int32_t header, char* buf,
+                                int64_t capacity, int64_t* length);
+
+/* ---- initial conditions in bulk ------------------------------------------
+ * Ephemeris::CalculatePhase with Ephemeris::KeplerEquationSolver
+ * (Solaris/Ephemeris.cpp:141-211) for n bodies on the device, one thread per
+ * body: elements[6n] = {a, e, i, argument of pericentre, longitude of node,
+ * mean anomaly} per body, mu[n] = G (m0 + m), phases[6n] = x y z vx vy vz.
+ * quirks: SOL_QUIRK_INT_ABS reproduces the reference build's stopping rule of
+ * the Kepler iteration (|change| through int abs(), so it stops once below 1);
+ * 0 iterates to 1e-14.  status[n] (may be NULL): SOL_OK or SOL_ERR_ORBIT where
+ * the iteration did not converge in 25 steps. */
+int sol_phases_from_elements(int32_t device, int32_t n, const double* mu, const double* elements, int32_t quirks,
+                             double* phases, int32_t* status);
+
 /* ---- discrete adjoint of fixed-step RKF78 --------------------------------
  * Forward: n_steps RungeKuttaFehlberg78::Step calls at constant h, each taking
  * the 7th-order result (RungeKuttaFehlberg78.cpp:147-250; heliocentric

@@ -202,6 +202,16 @@ def _declare(lib):
                                              _PF64, _PF64]),
         "sol_get_driver_vectors": (C.c_int, [P, _PF64, _PF64, _PF64]),
         "sol_get_side_buffers": (C.c_int, [P, _PF64, _PF64, _PF64]),
+        "sol_output_open": (C.c_int, [P, C.c_char_p, C.c_char_p, C.c_int32, C.POINTER(P)]),
+        "sol_output_save_phases": (C.c_int, [P, C.c_double]),
+        "sol_output_save_integrals": (C.c_int, [P, C.c_double]),
+        "sol_output_flush": (C.c_int, [P]),
+        "sol_output_close": (C.c_int, [P]),
+        "sol_format_phases_record": (C.c_int, [C.c_double, C.c_int32, _PF64, _PI32, C.c_int32, C.c_char_p,
+                                               C.c_int64, C.POINTER(C.c_int64)]),
+        "sol_format_integrals_record": (C.c_int, [C.c_double, C.c_int32, _PF64, C.c_int32, C.c_char_p, C.c_int64,
+                                                  C.POINTER(C.c_int64)]),
+        "sol_phases_from_elements": (C.c_int, [C.c_int32, C.c_int32, _PF64, _PF64, C.c_int32, _PF64, _PI32]),
         "sol_gravity_noalloc": (C.c_int, [C.POINTER(SolNBodies), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     }
@@ -224,7 +234,9 @@ def exported_names():
         "sol_ensemble_set_state", "sol_ensemble_get_state", "sol_ensemble_advance", "sol_ensemble_configure",
         "sol_ensemble_autotune", "sol_adjoint_forward", "sol_adjoint_backward", "sol_set_masses",
         "sol_accel_term", "sol_migration_helper", "sol_error_max", "sol_integrator_attempt",
-        "sol_get_driver_vectors", "sol_get_side_buffers", "sol_bench_stages"]
+        "sol_get_driver_vectors", "sol_get_side_buffers", "sol_bench_stages", "sol_output_open",
+        "sol_output_save_phases", "sol_output_save_integrals", "sol_output_flush", "sol_output_close",
+        "sol_format_phases_record", "sol_format_integrals_record", "sol_phases_from_elements"]
 
 
 def load_library(path: str | None = None):

@@ -146,6 +146,7 @@ void free_ctx(sol_ctx* c) {
   for (int k = 0; k < 2; ++k) sol_graph_release(c->graphs[k]);
   sol_adjoint_free(c->adj);
   if (c->d_persist) cudaFree(c->d_persist);
+  free(c->h_id);
   if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -290,6 +291,12 @@ int sol_create(const sol_body_data* b, const sol_gas_component* gas, int32_t bar
     return fail(SOL_ERR_CUDA);
   }
   const size_t N = c->n, NV = c->nv;
+  c->h_id = (int32_t*)malloc(sizeof(int32_t) * N);
+  if (!c->h_id) {
+    sol_set_error("host allocation failed");
+    return fail(SOL_ERR_NOMEM);
+  }
+  for (size_t i = 0; i < N; ++i) c->h_id[i] = b->id ? b->id[i] : (int32_t)i;
   if ((rc = dev_alloc(&c->d_type, N)) || (rc = dev_alloc(&c->d_mig_type, N)) ||
       (rc = dev_alloc(&c->d_mig_stop_at, N)) || (rc = dev_alloc(&c->d_mass, N)) ||
       (rc = dev_alloc(&c->d_radius, N)) || (rc = dev_alloc(&c->d_density, N)) || (rc = dev_alloc(&c->d_cd, N)) ||

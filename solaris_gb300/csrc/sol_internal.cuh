@@ -168,6 +168,7 @@ struct sol_ctx {
   int graph_used;
   sol_adjoint_state* adj;  // checkpoints and buffers of the discrete adjoint
   double* d_persist;       // source tables, block maxima and barrier words of the persistent driver
+  int32_t* h_id;           // BodyData::id on the host (output records carry ids)
 };
 
 // ---- launch helpers (defined in sol_force.cu / sol_integrate.cu) --------------

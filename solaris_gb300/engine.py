@@ -239,3 +239,82 @@ def fp64_peak_flops(device: int = 0) -> float:
     v = C.c_double(0)
     abi.check(lib, lib.sol_measure_fp64_peak(int(device), C.byref(v)))
     return float(v.value)
+
+
+# -- output files (BinaryFileAdapter record layouts) -------------------------------
+class Output:
+    """Phases / integrals files of a context: records appended in the
+    reference's layout; phases snapshots are written by a background thread
+    while the integration continues."""
+
+    def __init__(self, ctx: "Context", phases: str | None = None, integrals: str | None = None,
+                 text: bool = False):
+        self.lib = ctx.lib
+        self.ctx = ctx
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.sol_output_open(ctx.h, phases.encode() if phases else None,
+                                                     integrals.encode() if integrals else None, int(text),
+                                                     C.byref(h)))
+        self.h = h
+
+    def save_phases(self, time: float):
+        abi.check(self.lib, self.lib.sol_output_save_phases(self.h, float(time)))
+
+    def save_integrals(self, time: float):
+        abi.check(self.lib, self.lib.sol_output_save_integrals(self.h, float(time)))
+
+    def flush(self):
+        abi.check(self.lib, self.lib.sol_output_flush(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            h, self.h = self.h, None
+            abi.check(self.lib, self.lib.sol_output_close(h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def format_phases_record(time: float, y, ids, text: bool = False) -> bytes:
+    lib = abi.load_library()
+    y = np.ascontiguousarray(y, np.float64)
+    ids = np.ascontiguousarray(ids, np.int32)
+    n = C.c_int64(0)
+    abi.check(lib, lib.sol_format_phases_record(float(time), len(ids), abi.f64p(y), abi.i32p(ids), int(text), None,
+                                                0, C.byref(n)))
+    buf = C.create_string_buffer(n.value)
+    abi.check(lib, lib.sol_format_phases_record(float(time), len(ids), abi.f64p(y), abi.i32p(ids), int(text), buf,
+                                                n.value, C.byref(n)))
+    return buf.raw[:n.value]
+
+
+def format_integrals_record(time: float, values, header: bool = False) -> bytes:
+    lib = abi.load_library()
+    v = np.ascontiguousarray(values, np.float64)
+    n = C.c_int64(0)
+    abi.check(lib, lib.sol_format_integrals_record(float(time), len(v), abi.f64p(v), int(header), None, 0,
+                                                   C.byref(n)))
+    buf = C.create_string_buffer(n.value)
+    abi.check(lib, lib.sol_format_integrals_record(float(time), len(v), abi.f64p(v), int(header), buf, n.value,
+                                                   C.byref(n)))
+    return buf.raw[:n.value]
+
+
+def phases_from_elements(mu, elements, quirks: int = abi.QUIRKS_REFERENCE, device: int = 0):
+    """Ephemeris::CalculatePhase for many bodies on the device: elements (n, 6)
+    = a, e, i, argument of pericentre, longitude of node, mean anomaly; mu (n,)
+    = G (m0 + m).  Returns phases (n, 6) and the per-body status."""
+    lib = abi.load_library()
+    mu = np.ascontiguousarray(mu, np.float64)
+    el = np.ascontiguousarray(elements, np.float64).reshape(-1, 6)
+    n = len(mu)
+    ph = np.empty((n, 6))
+    st = np.empty(n, np.int32)
+    rc = lib.sol_phases_from_elements(int(device), n, abi.f64p(mu), abi.f64p(el), int(quirks), abi.f64p(ph),
+                                      abi.i32p(st))
+    if rc not in (abi.SOL_OK, abi.SOL_ERR_ORBIT):
+        abi.check(lib, rc)
+    return ph, st
