@@ -325,6 +325,44 @@ int sol_format_phases_record(double time, int32_t n, const double* y, const int3
 int sol_format_integrals_record(double time, int32_t n, const double* integrals, int32_t header, char* buf,
                                 int64_t capacity, int64_t* length);
 
+/* ---- events on the device: Simulator::CheckEvent (Solaris/Simulator.cpp:
+ * 621-735) with RemoveBody (:737-771) and HandleCollision (:773-935) --------- */
+/* TwoBodyAffair (Solaris/TwoBodyAffair.h): type is the reference's EventType
+ * (0 ejection, 1 hit centrum, 3 collision); idx1/idx2 the bodies' indices
+ * (ejection and hit centrum: before any removal; collision: among the bodies
+ * present at that moment, survivor first); phases before a merge. */
+typedef struct sol_affair {
+  int32_t type;
+  int32_t idx1, idx2;
+  int32_t id1, id2;
+  int32_t pad;
+  double time;
+  double phase1[6];
+  double phase2[6];
+} sol_affair;
+/* After a driver call (the last evaluation's rm3 and nearest neighbours):
+ * every body with rm3 < 1/ejection^3 is logged and removed; every body with
+ * rm3 > 1/hit_centrum^3 is merged into the central body and removed; then,
+ * in body order, a body whose nearest neighbour j satisfies
+ * collision_factor * (R_i + R_j) > distance merges with it (the lighter into
+ * the heavier, equal masses into the lower index; mass and momentum add up,
+ * radius from the summed volume) and the merger is removed.  A parameter <= 0
+ * turns that event off.  The context's bodies are compacted on the device
+ * (counts, parameters, state, side buffers); nearest neighbours are cleared
+ * until the next evaluation.  log receives up to capacity affairs, *n_log
+ * their number.  Bodies are identified by id where the reference uses
+ * indices that earlier removals have shifted. */
+int sol_handle_events(sol_ctx* ctx, double time, double ejection, double hit_centrum, double collision_factor,
+                      sol_affair* log, int32_t capacity, int32_t* n_log);
+/* The context's body set: counts, ids, types and the (possibly merged)
+ * mass, radius and density; any pointer may be NULL. */
+int sol_get_bodies(sol_ctx* ctx, sol_nbodies* counts, int32_t* id, int32_t* type, double* mass, double* radius,
+                   double* density);
+/* SaveTwoBodyAffair (Solaris/BinaryFileAdapter.cpp:244-261): appends n
+ * records (int32 event id = first_event_id + k, int32 type, int32 body ids,
+ * 6 + 6 doubles of phases, double time) to path. */
+int sol_write_affairs(const char* path, const sol_affair* affairs, int32_t n, int32_t first_event_id);
+
 /* ---- initial conditions in bulk ------------------------------------------
  * Ephemeris::CalculatePhase with Ephemeris::KeplerEquationSolver
  * (Solaris/Ephemeris.cpp:141-211) for n bodies on the device, one thread per

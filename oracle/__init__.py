@@ -75,6 +75,9 @@ def load():
         lib.orc_jvp.argtypes = [P, F, F, F, F]
         lib.orc_rkf78_fixed.argtypes = [P, F, C.c_double, C.c_int32, F, F, F, F]
         lib.orc_set_masses.argtypes = [P, F]
+        lib.orc_get_bodies.argtypes = [P, C.POINTER(abi.SolNBodies), I, I, F, F, F]
+        lib.orc_handle_events.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double, F,
+                                          C.POINTER(abi.SolAffair), C.c_int32, C.POINTER(C.c_int32)]
         lib.orc_gravity_ac_sample.restype = C.c_int64
         lib.orc_gravity_ac_sample.argtypes = [P, F, C.c_int32, C.c_int32, F, C.c_int32]
         _lib = lib
@@ -169,6 +172,26 @@ class Oracle:
         dmp = abi.f64p(np.ascontiguousarray(dm, np.float64)) if dm is not None else None
         self.lib.orc_rkf78_fixed(self.h, abi.f64p(y0), h, n_steps, abi.f64p(y), dyp, dmp, abi.f64p(dyo))
         return (y, dyo) if dy0 is not None else y
+
+    def handle_events(self, time, y0, ejection=0.0, hit_centrum=0.0, collision_factor=0.0):
+        """Events on the last evaluation; returns the compacted y0 and the affairs."""
+        y = np.array(y0, dtype=np.float64, copy=True)
+        arr = (abi.SolAffair * max(self.n, 1))()
+        k = C.c_int32(0)
+        self.lib.orc_handle_events(self.h, float(time), float(ejection), float(hit_centrum), float(collision_factor),
+                                   abi.f64p(y), arr, self.n, C.byref(k))
+        self.n = int(self.lib.orc_n_total(self.h))
+        return y[:6 * self.n].copy(), abi.affairs_to_list(arr, k.value)
+
+    def bodies(self):
+        n = self.n
+        counts = abi.SolNBodies()
+        ids, types = np.empty(n, np.int32), np.empty(n, np.int32)
+        mass, radius, density = np.empty(n), np.empty(n), np.empty(n)
+        self.lib.orc_get_bodies(self.h, C.byref(counts), abi.i32p(ids), abi.i32p(types), abi.f64p(mass),
+                                abi.f64p(radius), abi.f64p(density))
+        return dict(counts=tuple(getattr(counts, f) for f, _ in abi.SolNBodies._fields_), id=ids, type=types,
+                    mass=mass, radius=radius, density=density)
 
     def gravity_sample(self, y, i_begin, i_end, n_threads=1):
         y = np.ascontiguousarray(y, dtype=np.float64)

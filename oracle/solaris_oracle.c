@@ -1139,3 +1139,171 @@ int orc_rkf78_fixed(orc_system* s, const double* y0, double h, int32_t n_steps, 
 }
 
 void orc_set_masses(orc_system* s, const double* mass) { memcpy(s->mass, mass, sizeof(double) * s->total); }
+
+/* ---- events: Simulator::CheckEvent (Simulator.cpp:621-735), RemoveBody
+ * (:737-771), HandleCollision (:773-935) ---------------------------------------
+ * The reference's order and arithmetic, with bodies identified by identity
+ * where the reference indexes arrays that earlier removals have shifted, and
+ * every per-body array compacted (RemoveBody shifts only some of them): the
+ * semantics the device implementation documents. */
+static int ev_position(const char* removed, int b) {
+  int p = 0;
+  for (int q = 0; q < b; ++q) p += !removed[q];
+  return p;
+}
+
+static void ev_log(orc_system* s, const double* y0, sol_affair* log, int cap, int* nl, int type, int idx1, int idx2,
+                   int b1, int b2, double time) {
+  if (*nl < cap) {
+    sol_affair* f = &log[*nl];
+    f->type = type;
+    f->idx1 = idx1;
+    f->idx2 = idx2;
+    f->id1 = s->id[b1];
+    f->id2 = s->id[b2];
+    f->pad = 0;
+    f->time = time;
+    for (int q = 0; q < 6; ++q) {
+      f->phase1[q] = y0[6 * b1 + q];
+      f->phase2[q] = y0[6 * b2 + q];
+    }
+  }
+  (*nl)++;
+}
+
+static void ev_survivor(const orc_system* s, int a, int b, int* sv, int* mg) {  /* :775-781 */
+  if (s->mass[a] == s->mass[b]) {
+    *sv = a < b ? a : b;
+    *mg = a > b ? a : b;
+  } else {
+    *sv = s->mass[a] > s->mass[b] ? a : b;
+    *mg = s->mass[a] < s->mass[b] ? a : b;
+  }
+}
+
+static void ev_merge(orc_system* s, double* y0, int sv, int mg) {  /* :799-880 */
+  double ms = s->mass[sv];
+  double mm = s->type[mg] == SOL_SUPER_PLANETESIMAL
+                  ? s->density[mg] * (4.0 / 3.0 * K_PI * (s->radius[mg] * s->radius[mg] * s->radius[mg]))
+                  : s->mass[mg];
+  double M = ms + mm;
+  if (s->type[sv] != SOL_CENTRAL_BODY)
+    for (int q = 0; q < 6; ++q) y0[6 * sv + q] = 1.0 / M * (ms * y0[6 * sv + q] + mm * y0[6 * mg + q]);
+  s->mass[sv] = M;
+  if (s->radius[sv] == 0.0) return;
+  if (s->radius[mg] == 0.0) {
+    s->density[mg] = s->density[sv];
+    s->radius[mg] = pow(3.0 / (4.0 * K_PI) * s->mass[mg] / s->density[mg], 1.0 / 3.0);
+  }
+  double rs = s->radius[sv], rm = s->radius[mg];
+  double vol = 4.0 / 3.0 * K_PI * (rs * rs * rs + rm * rm * rm);
+  s->radius[sv] = pow(3.0 / (4.0 * K_PI) * vol, 1.0 / 3.0);
+  s->density[sv] = M / vol;
+}
+
+static void compact_d(double* a, const char* removed, int n, int width) {
+  int k = 0;
+  for (int i = 0; i < n; ++i)
+    if (!removed[i]) {
+      if (k != i) memmove(a + (size_t)k * width, a + (size_t)i * width, sizeof(double) * width);
+      k++;
+    }
+}
+static void compact_i(int32_t* a, const char* removed, int n) {
+  int k = 0;
+  for (int i = 0; i < n; ++i)
+    if (!removed[i]) a[k++] = a[i];
+}
+static void compact_rows(double* buf, const char* removed, int lo, int hi) {
+  int k = 0;
+  for (int i = lo; i < hi; ++i)
+    if (!removed[i]) {
+      if (k != i - lo) memmove(buf + 3 * k, buf + 3 * (i - lo), 3 * sizeof(double));
+      k++;
+    }
+}
+
+int orc_handle_events(orc_system* s, double time, double ejection, double hit_centrum, double factor, double* y0,
+                      sol_affair* log, int32_t cap, int32_t* n_log) {
+  const int n = s->total;
+  char* removed = (char*)calloc(n > 0 ? n : 1, 1);
+  double e3 = ejection > 0 ? 1.0 / (ejection * ejection * ejection) : 0.0;
+  double h3 = hit_centrum > 0 ? 1.0 / (hit_centrum * hit_centrum * hit_centrum) : 0.0;
+  int nl = 0;
+  for (int i = 1; i < n; ++i)  /* ejections (:631-637, :648-659) */
+    if (ejection > 0 && s->rm3[i] < e3) {
+      ev_log(s, y0, log, cap, &nl, 0, 0, i, 0, i, time);
+      removed[i] = 1;
+    }
+  for (int i = 1; i < n; ++i)  /* hit centrum (:639-645, :661-687) */
+    if (!removed[i] && hit_centrum > 0 && s->rm3[i] > h3) {
+      ev_log(s, y0, log, cap, &nl, 1, 0, i, 0, i, time);
+      int sv, mg;
+      ev_survivor(s, 0, i, &sv, &mg);
+      if (s->type[mg] != SOL_TEST_PARTICLE) ev_merge(s, y0, sv, mg);
+      removed[i] = 1;
+    }
+  if (factor > 0)  /* collisions (:689-732) */
+    for (int i = 0; i < n; ++i) {
+      if (removed[i]) continue;
+      int j = s->nn_idx[i];
+      if (j < 0 || removed[j] || !(factor * (s->radius[i] + s->radius[j]) > s->nn_dist[i])) continue;
+      int sv, mg;
+      ev_survivor(s, i, j, &sv, &mg);
+      if (s->type[mg] == SOL_TEST_PARTICLE) {
+        s->nn_idx[i] = -1;
+        continue;
+      }
+      ev_log(s, y0, log, cap, &nl, 3, ev_position(removed, sv), ev_position(removed, mg), sv, mg, time);
+      ev_merge(s, y0, sv, mg);
+      removed[mg] = 1;
+      s->nn_idx[mg] = -1;
+    }
+  int nr = 0;
+  for (int i = 0; i < n; ++i) nr += removed[i];
+  if (nr > 0) {
+    const int nm_old = n_massive(s), nc_old = s->n.central_body, ng_old = s->n.giant_planet;
+    const int hi_drag = nm_old + n_pl_and_spl(s);
+    if (s->acc_drag) compact_rows(s->acc_drag, removed, nm_old, hi_drag);
+    if (s->acc_mig1) compact_rows(s->acc_mig1, removed, nc_old + ng_old, nm_old);
+    if (s->acc_mig2) compact_rows(s->acc_mig2, removed, nc_old, nc_old + ng_old);
+    for (int i = 0; i < n; ++i) {
+      if (!removed[i]) continue;
+      switch (s->type[i]) {
+        case SOL_CENTRAL_BODY: s->n.central_body--; break;
+        case SOL_GIANT_PLANET: s->n.giant_planet--; break;
+        case SOL_ROCKY_PLANET: s->n.rocky_planet--; break;
+        case SOL_PROTO_PLANET: s->n.proto_planet--; break;
+        case SOL_SUPER_PLANETESIMAL: s->n.super_planetesimal--; break;
+        case SOL_PLANETESIMAL: s->n.planetesimal--; break;
+        default: s->n.test_particle--; break;
+      }
+    }
+    compact_i(s->id, removed, n);
+    compact_i(s->type, removed, n);
+    compact_i(s->mig_type, removed, n);
+    double* per_body[] = {s->mig_stop_at, s->mass, s->radius, s->density, s->cd, s->gamma_stokes, s->gamma_epstein,
+                          s->rm3};
+    for (int k = 0; k < 8; ++k) compact_d(per_body[k], removed, n, 1);
+    compact_d(y0, removed, n, 6);
+    s->total = n - nr;
+    for (int i = 0; i < s->total; ++i) {
+      s->nn_idx[i] = -1;
+      s->nn_dist[i] = 0.0;
+    }
+  }
+  free(removed);
+  *n_log = nl;
+  return 0;
+}
+
+void orc_get_bodies(const orc_system* s, sol_nbodies* counts, int32_t* id, int32_t* type, double* mass,
+                    double* radius, double* density) {
+  const size_t n = (size_t)s->total;
+  if (counts) *counts = s->n;
+  if (id) memcpy(id, s->id, sizeof(int32_t) * n);
+  if (type) memcpy(type, s->type, sizeof(int32_t) * n);
+  if (mass) memcpy(mass, s->mass, sizeof(double) * n);
+  if (radius) memcpy(radius, s->radius, sizeof(double) * n);
+  if (density) memcpy(density, s->density, sizeof(double) * n);
+}

@@ -66,6 +66,14 @@ int orc_rkf78_fixed(orc_system* s, const double* y0, double h, int32_t n_steps, 
                     const double* dm, double* dy_out);
 void orc_set_masses(orc_system* s, const double* mass);
 
+/* Simulator::CheckEvent with RemoveBody and HandleCollision (Simulator.cpp:
+ * 621-935) on the last evaluation's rm3 and nearest neighbours: y0 and the
+ * system are compacted in place; *n_log affairs (up to cap in log). */
+int orc_handle_events(orc_system* s, double time, double ejection, double hit_centrum, double factor, double* y0,
+                      sol_affair* log, int32_t cap, int32_t* n_log);
+void orc_get_bodies(const orc_system* s, sol_nbodies* counts, int32_t* id, int32_t* type, double* mass,
+                    double* radius, double* density);
+
 #ifdef __cplusplus
 }
 #endif

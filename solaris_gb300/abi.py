@@ -78,6 +78,12 @@ class SolGasComponent(C.Structure):
                 ("scale_height", SolPowerLaw), ("density", SolPowerLaw), ("mean_free_path", SolPowerLaw)]
 
 
+class SolAffair(C.Structure):
+    _fields_ = [("type", C.c_int32), ("idx1", C.c_int32), ("idx2", C.c_int32), ("id1", C.c_int32),
+                ("id2", C.c_int32), ("pad", C.c_int32), ("time", C.c_double), ("phase1", C.c_double * 6),
+                ("phase2", C.c_double * 6)]
+
+
 class SolTimeLine(C.Structure):
     _fields_ = [("time", C.c_double), ("h_next", C.c_double), ("h_did", C.c_double)]
 
@@ -212,6 +218,10 @@ def _declare(lib):
         "sol_format_integrals_record": (C.c_int, [C.c_double, C.c_int32, _PF64, C.c_int32, C.c_char_p, C.c_int64,
                                                   C.POINTER(C.c_int64)]),
         "sol_phases_from_elements": (C.c_int, [C.c_int32, C.c_int32, _PF64, _PF64, C.c_int32, _PF64, _PI32]),
+        "sol_handle_events": (C.c_int, [P, C.c_double, C.c_double, C.c_double, C.c_double, C.POINTER(SolAffair),
+                                        C.c_int32, C.POINTER(C.c_int32)]),
+        "sol_get_bodies": (C.c_int, [P, C.POINTER(SolNBodies), _PI32, _PI32, _PF64, _PF64, _PF64]),
+        "sol_write_affairs": (C.c_int, [C.c_char_p, C.POINTER(SolAffair), C.c_int32, C.c_int32]),
         "sol_gravity_noalloc": (C.c_int, [C.POINTER(SolNBodies), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     }
@@ -236,7 +246,8 @@ def exported_names():
         "sol_accel_term", "sol_migration_helper", "sol_error_max", "sol_integrator_attempt",
         "sol_get_driver_vectors", "sol_get_side_buffers", "sol_bench_stages", "sol_output_open",
         "sol_output_save_phases", "sol_output_save_integrals", "sol_output_flush", "sol_output_close",
-        "sol_format_phases_record", "sol_format_integrals_record", "sol_phases_from_elements"]
+        "sol_format_phases_record", "sol_format_integrals_record", "sol_phases_from_elements",
+        "sol_handle_events", "sol_get_bodies", "sol_write_affairs"]
 
 
 def load_library(path: str | None = None):
@@ -265,3 +276,8 @@ def check(lib, rc):
         msg = lib.sol_last_error()
         raise SolError(rc, msg.decode() if msg else "")
     return rc
+
+
+def affairs_to_list(arr, n):
+    return [dict(type=a.type, idx1=a.idx1, idx2=a.idx2, id1=a.id1, id2=a.id2, time=a.time,
+                 phase1=np.array(a.phase1[:]), phase2=np.array(a.phase2[:])) for a in arr[:n]]

@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const doubl
     nn[s] = -1;
   }
   // accumulator state (warp 0, lanes < kFewTerms): lane = component * kFewSinks + sink
-  const int a_s = lane % kFewSinks, a_c = lane / kFewSinks;
+  const int a_s = lane % kFewSinks;
   const int a_i = i0 + a_s;
   const int a_ns = (lane < kFewTerms) ? sink_ns[a_s] : 0;
   double a_sum = 0.0;

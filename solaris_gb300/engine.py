@@ -126,6 +126,30 @@ class Context:
         abi.check(self.lib, self.lib.sol_bench_force(self.h, int(precision), int(reps), C.byref(ms)))
         return float(ms.value)
 
+    # -- events ---------------------------------------------------------------
+    def handle_events(self, time, ejection=0.0, hit_centrum=0.0, collision_factor=0.0):
+        """Simulator::CheckEvent on the device: removals and merges compact the
+        context's bodies.  Returns the affairs (TwoBodyAffair) in order."""
+        cap = self.n
+        arr = (abi.SolAffair * max(cap, 1))()
+        k = C.c_int32(0)
+        abi.check(self.lib, self.lib.sol_handle_events(self.h, float(time), float(ejection), float(hit_centrum),
+                                                       float(collision_factor), arr, cap, C.byref(k)))
+        counts = abi.SolNBodies()
+        self.lib.sol_get_bodies(self.h, C.byref(counts), None, None, None, None, None)
+        self.n = int(sum(getattr(counts, f) for f, _ in abi.SolNBodies._fields_))
+        return abi.affairs_to_list(arr, k.value)
+
+    def bodies(self):
+        n = self.n
+        counts = abi.SolNBodies()
+        ids, types = np.empty(n, np.int32), np.empty(n, np.int32)
+        mass, radius, density = np.empty(n), np.empty(n), np.empty(n)
+        abi.check(self.lib, self.lib.sol_get_bodies(self.h, C.byref(counts), abi.i32p(ids), abi.i32p(types),
+                                                    abi.f64p(mass), abi.f64p(radius), abi.f64p(density)))
+        return dict(counts=tuple(getattr(counts, f) for f, _ in abi.SolNBodies._fields_), id=ids, type=types,
+                    mass=mass, radius=radius, density=density)
+
     # -- discrete adjoint ---------------------------------------------------------
     def set_masses(self, mass):
         m = np.ascontiguousarray(mass, dtype=np.float64)
