@@ -75,6 +75,9 @@ def load():
         lib.orc_jvp.argtypes = [P, F, F, F, F]
         lib.orc_rkf78_fixed.argtypes = [P, F, C.c_double, C.c_int32, F, F, F, F]
         lib.orc_set_masses.argtypes = [P, F]
+        lib.orc_gas_probe.restype = C.c_double
+        lib.orc_gas_probe.argtypes = [C.POINTER(abi.SolGasComponent), C.c_int32, F, F]
+        lib.orc_kepler_solve.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int32, F]
         lib.orc_get_bodies.argtypes = [P, C.POINTER(abi.SolNBodies), I, I, F, F, F]
         lib.orc_handle_events.argtypes = [P, C.c_double, C.c_double, C.c_double, C.c_double, F,
                                           C.POINTER(abi.SolAffair), C.c_int32, C.POINTER(C.c_int32)]
@@ -221,3 +224,20 @@ def orbital_element(mu, phase, quirks=abi.QUIRKS_REFERENCE):
     a, e = np.zeros(1), np.zeros(1)
     rc = lib.orc_calculate_orbital_element(mu, abi.f64p(ph), abi.f64p(a), abi.f64p(e), quirks)
     return rc, float(a[0]), float(e[0])
+
+
+def gas_probe(gas: dict, which: int, *args):
+    """GasComponent helpers of the oracle: (value, vector)."""
+    lib = load()
+    g = abi.gas_struct(gas)
+    a = np.ascontiguousarray(args, dtype=np.float64)
+    out = np.zeros(3)
+    v = lib.orc_gas_probe(C.byref(g), int(which), abi.f64p(a), abi.f64p(out))
+    return float(v), out
+
+
+def kepler_solve(e, m, eps=1e-14, quirks=0):
+    lib = load()
+    E = np.zeros(1)
+    rc = lib.orc_kepler_solve(e, m, eps, int(quirks), abi.f64p(E))
+    return rc, float(E[0])

@@ -1307,3 +1307,61 @@ void orc_get_bodies(const orc_system* s, sol_nbodies* counts, int32_t* id, int32
   if (radius) memcpy(radius, s->radius, sizeof(double) * n);
   if (density) memcpy(density, s->density, sizeof(double) * n);
 }
+
+/* ---- GasComponent helpers, for their known-answer tests ------------------- */
+/* which: 0 circular_velocity(mu, r) -> out[3]; 1 gas_velocity(mu, r) -> out[3];
+ * 2 gas_density_at(r); 3 MeanFreePath_CMU(rho); 4 SoundSpeed_CMU(T);
+ * 5 Temperature_CMU(mC, r); 6 MeanThermalSpeed_CMU(mC, r) as the drag calls it
+ * (GasComponent.cpp:97-157, :159-243). */
+double orc_gas_probe(const sol_gas_component* g, int32_t which, const double* args, double* out3) {
+  switch (which) {
+    case 0: circular_velocity(args[0], args + 1, out3); return 0.0;
+    case 1: gas_velocity(g, args[0], args + 1, out3); return 0.0;
+    case 2: return gas_density_at(g, args);
+    case 3: {  /* MeanFreePath_CMU (:170-188) */
+      const double sqrt_two_pi = 4.4428829381583662470158809900607;  /* the value of the reference's constant */
+      double a1 = g->mean_molecular_weight * c_proton_mass_cmu();
+      double d2 = SQR(g->particle_diameter * c_meter_to_au());
+      double result = a1 / sqrt_two_pi;
+      return result / (d2 * args[0]);
+    }
+    case 4: {  /* SoundSpeed_CMU (:198-204) */
+      double result = c_boltzman_cmu() * args[0];
+      result /= g->mean_molecular_weight * c_proton_mass_cmu();
+      return sqrt(result);
+    }
+    case 5: {  /* Temperature_CMU (:221-229) */
+      double cTp = K_GAUSS2 * c_proton_mass_boltzman_cmu();
+      double pT = 2.0 * g->scale_height.index - 3.0;
+      double cT = SQR(g->scale_height.c) * args[0] * g->mean_molecular_weight * cTp;
+      return cT * pow(args[1], pT);
+    }
+    case 6: {
+      orc_system tmp;
+      memset(&tmp, 0, sizeof(tmp));
+      tmp.gas = *g;
+      return mean_thermal_speed_cmu(&tmp, args[0], args[1]);
+    }
+    default: return 0.0;
+  }
+}
+
+/* KeplerEquationSolver with the stopping rule selectable: SOL_QUIRK_INT_ABS
+ * as the reference build, 0 with fabs (as the reference's CUDA prototypes). */
+int orc_kepler_solve(double e, double m, double eps, int32_t quirks, double* E) {
+  if (e == 0.0 || m == 0.0 || m == K_PI) {
+    *E = m;
+    return 0;
+  }
+  double EE = m + e * (sin(m)) / (1.0 - sin(m + e) + sin(m));
+  double E1 = 0.0, error;
+  int step = 0;
+  do {
+    E1 = EE - (EE - e * sin(EE) - m) / (1.0 - e * cos(EE));
+    error = quirk_abs(E1 - EE, quirks);
+    EE = E1;
+    step++;
+  } while (error > eps && step <= 25);
+  *E = EE;
+  return step > 25 ? 1 : 0;
+}

@@ -71,6 +71,8 @@ void orc_set_masses(orc_system* s, const double* mass);
  * system are compacted in place; *n_log affairs (up to cap in log). */
 int orc_handle_events(orc_system* s, double time, double ejection, double hit_centrum, double factor, double* y0,
                       sol_affair* log, int32_t cap, int32_t* n_log);
+double orc_gas_probe(const sol_gas_component* g, int32_t which, const double* args, double* out3);
+int orc_kepler_solve(double e, double m, double eps, int32_t quirks, double* E);
 void orc_get_bodies(const orc_system* s, sol_nbodies* counts, int32_t* id, int32_t* type, double* mass,
                     double* radius, double* density);
 
