@@ -241,3 +241,56 @@ def kepler_solve(e, m, eps=1e-14, quirks=0):
     E = np.zeros(1)
     rc = lib.orc_kepler_solve(e, m, eps, int(quirks), abi.f64p(E))
     return rc, float(E[0])
+
+
+class ScenarioBackend:
+    """The oracle behind solaris_gb300.simulator.Simulator: one Driver call per
+    step on the host, events by orc_handle_events, records formatted by the
+    library's BinaryFileAdapter layouts (test infrastructure: the checker of
+    the device run of a scenario file)."""
+
+    def __init__(self, scenario, directory):
+        from solaris_gb300 import engine
+        st = scenario.settings
+        self.fmt_phases, self.fmt_integrals = engine.format_phases_record, engine.format_integrals_record
+        self.o = Oracle(scenario.system)
+        self.y0 = np.array(scenario.system.y0, dtype=np.float64, copy=True)
+        self.integrator = st.integrator
+        self.phases = os.path.join(directory, st.phases)
+        self.integrals_path = os.path.join(directory, st.integrals)
+        self.first_integrals = True
+
+    def step(self, time, h_next):
+        r = self.o.driver(self.integrator, self.y0, time, h_next, 1)
+        if r["status"] != 0:
+            raise RuntimeError(f"oracle driver status {r['status']}")
+        self.y0 = r["y0"]
+        t, hn, hd = r["tl"]
+        return t, hd, hn
+
+    def events(self, time, ejection, hit_centrum, collision_factor):
+        self.y0, affairs = self.o.handle_events(time, self.y0, ejection, hit_centrum, collision_factor)
+        return affairs
+
+    def n_total(self):
+        return self.o.n
+
+    def state(self):
+        return self.y0.copy()
+
+    def zero_below_smallest(self):
+        self.y0[np.abs(self.y0) < 1.0e-50] = 0.0
+
+    def save_phases(self, time):
+        ids = self.o.bodies()["id"]
+        with open(self.phases, "ab") as f:
+            f.write(self.fmt_phases(time, self.y0, ids))
+
+    def save_integrals(self, time):
+        rec = self.fmt_integrals(time, self.o.integrals(self.y0), header=self.first_integrals)
+        self.first_integrals = False
+        with open(self.integrals_path, "ab") as f:
+            f.write(rec)
+
+    def close(self):
+        pass
