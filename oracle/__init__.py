@@ -249,16 +249,14 @@ class ScenarioBackend:
     library's BinaryFileAdapter layouts (test infrastructure: the checker of
     the device run of a scenario file)."""
 
-    def __init__(self, scenario, directory):
+    def __init__(self, system, st, directory):
         from solaris_gb300 import engine
-        st = scenario.settings
         self.fmt_phases, self.fmt_integrals = engine.format_phases_record, engine.format_integrals_record
-        self.o = Oracle(scenario.system)
-        self.y0 = np.array(scenario.system.y0, dtype=np.float64, copy=True)
+        self.o = Oracle(system)
+        self.y0 = np.array(system.y0, dtype=np.float64, copy=True)
         self.integrator = st.integrator
         self.phases = os.path.join(directory, st.phases)
         self.integrals_path = os.path.join(directory, st.integrals)
-        self.first_integrals = True
 
     def step(self, time, h_next):
         r = self.o.driver(self.integrator, self.y0, time, h_next, 1)
@@ -287,8 +285,8 @@ class ScenarioBackend:
             f.write(self.fmt_phases(time, self.y0, ids))
 
     def save_integrals(self, time):
-        rec = self.fmt_integrals(time, self.o.integrals(self.y0), header=self.first_integrals)
-        self.first_integrals = False
+        first = not os.path.exists(self.integrals_path) or os.path.getsize(self.integrals_path) == 0
+        rec = self.fmt_integrals(time, self.o.integrals(self.y0), header=first)
         with open(self.integrals_path, "ab") as f:
             f.write(rec)
 

@@ -115,6 +115,9 @@ class Settings:
     hit_centrum: float = 0.0  # AU, 0: off
     collision: float | None = None  # factor; None: no Collision element
     h0: float = 0.0           # first step of the main integration
+    start: float = 0.0        # TimeLine start (days), else the last (forward) or first epoch
+    start_defined: bool = False
+    enable_distinct_start_times: bool = False
 
 
 @dataclass
@@ -159,6 +162,10 @@ class Scenario:
     bodies: list            # BodySpec, in integration order
     system: scenarios.System
     insertion: list         # body ids in the order Simulator::Insert writes their properties
+    groups: list            # BodyGroup, ordered by start time (reversed for a backward run)
+    time0: float            # the time line's time: the start time of the first group with massive bodies
+    n_distinct_start_times: int
+    gas: dict | None
 
 
 # ---- attribute handling ------------------------------------------------------------
@@ -238,8 +245,8 @@ def _read_settings(se) -> Settings:
             raise ScenarioError(f"Invalid value: {key}={a[key]!r}")
         if key == "barycentric":
             st.barycentric = v == "true"
-        elif v == "true":
-            raise ScenarioError("distinct start times (enableDistinctStartTimes) are not supported")
+        else:
+            st.enable_distinct_start_times = v == "true"
     out = se.find("Output")
     if out is not None:
         for tag, key in (("Phases", "phases"), ("ConstantProperties", "constant_properties"),
@@ -272,7 +279,8 @@ def _read_settings(se) -> Settings:
     ta = _attrs(tl, ("start", "length", "output", "unit"))
     tu = _unit_attr(ta, "unit", TIME_UNITS, "", "day", tl)
     if "start" in ta:
-        raise ScenarioError("a TimeLine start (the pre-integration phase) is not supported")
+        st.start = _convert(_double(ta, "start", tl), tu, TIME_UNITS)
+        st.start_defined = True
     if "length" in ta:
         length = _double(ta, "length", tl)
         if length == 0.0:
@@ -326,7 +334,7 @@ def _power_law(el, current: tuple) -> tuple:
     return (c, idx)
 
 
-def _read_gas(gc) -> dict:
+def _read_gas(gc, legacy_gas_tags: bool = False) -> dict:
     """DeserializeGasComponent (:1900-2170) over GasComponent's defaults; the
     mean free path keeps the default density's value."""
     gas = scenarios.default_gas()
@@ -354,13 +362,16 @@ def _read_gas(gc) -> dict:
         e = gc.find(tag)
         if e is not None:
             gas[key] = _power_law(e, gas[key])
-    df = gc.find("DensityFunction")
-    if df is not None:
+    for tag, child in (("DensityFunction", "Density"),) + ((("GasDensityFunction", "VolumeDensity"),)
+                                                             if legacy_gas_tags else ()):
+        df = gc.find(tag)
+        if df is None:
+            continue
         c, idx = gas["density"]
         da = _attrs(df, ("index",))
         if "index" in da:
             idx = _double(da, "index", df)
-        d = df.find("Density")
+        d = df.find(child)
         if d is not None:
             c = _Quantity().read(d, VOLUME_DENSITY_UNITS, "solarau3")
         gas["density"] = (c, idx)
@@ -523,9 +534,79 @@ def _read_body(el, bid: int, group: int) -> BodySpec:
     return b
 
 
+# ---- epochs (Ephemeris::GetJulianDate and friends, Ephemeris.cpp:247-462) -----------------
+def _atof(text: str) -> float:
+    k = 0
+    while k < len(text) and (text[k].isdigit() or text[k] == "."):
+        k += 1
+    head = text[:k]
+    while head:
+        try:
+            return float(head)
+        except ValueError:
+            head = head[:-1]
+    return 0.0
+
+
+def _atoi(text: str) -> int:
+    k = 0
+    while k < len(text) and text[k].isdigit():
+        k += 1
+    return int(text[:k]) if k else 0
+
+
+def _to_julian_date(year: int, month: int, day: int) -> float:
+    """Ephemeris::ToJulianDate (Ephemeris.cpp:394-424) at 0h UT."""
+    y = year - 1 if month <= 2 else year
+    m = month + 12 if month <= 2 else month
+    if year < 1582 or (year == 1582 and month < 10) or (year == 1582 and month == 10 and day <= 4):
+        b = -2
+    else:
+        b = math.floor(y / 400.0) - math.floor(y / 100.0)
+    universal_time = 0 / 3600000.0 + 0 / 3600.0 + 0 / 60.0 + 0
+    return (math.floor(365.25 * y) + math.floor(30.6001 * (m + 1)) + b) + 1720996.5 + day + universal_time / 24.0
+
+
+def julian_date(epoch: str) -> float:
+    """An epoch as the reference reads it: 'JD2451545.0' (a Julian date),
+    'YYYYMMDD' (a date, at most 8 digits) or a 5-character packed date
+    ('K0101': century letter I-K, two digits of the year, month 1-9 / A-C,
+    day 1-9 / A-V)."""
+    if epoch[:2].lower() == "jd":
+        if not all(c.isdigit() or c == "." for c in epoch[2:]):
+            raise ScenarioError(f"Bad JulianDate format: {epoch}")
+        return _atof(epoch[2:])
+    if epoch[:1].isdigit():
+        if len(epoch) > 8 or not epoch.isdigit():
+            raise ScenarioError(f"Bad Date format: {epoch}")
+        return _to_julian_date(_atoi(epoch[0:4]), _atoi(epoch[4:6]), _atoi(epoch[6:8]))
+    if (len(epoch) != 5 or not "I" <= epoch[0] <= "K" or not epoch[1:3].isdigit()
+            or not (epoch[3].isdigit() or "A" <= epoch[3] <= "C")
+            or not (epoch[4].isdigit() or "A" <= epoch[4] <= "V")):
+        raise ScenarioError(f"Bad PackedDate format: {epoch}")
+    year = (ord(epoch[0]) - ord("I") + 18) * 100 + _atoi(epoch[1:3])
+    month = int(epoch[3]) if epoch[3].isdigit() else ord(epoch[3]) - ord("A") + 10
+    day = int(epoch[4]) if epoch[4].isdigit() else ord(epoch[4]) - ord("A") + 10
+    return _to_julian_date(year, month, day)
+
+
 # ---- the simulation -------------------------------------------------------------------------
-def load(path: str) -> Scenario:
-    """Read and prepare a scenario file; raises ScenarioError where the reference reports an error."""
+@dataclass
+class BodyGroup:
+    description: str
+    epoch: str
+    offset: float
+    reference_frame: str
+    bodies: list
+    start_time: float = 0.0
+
+
+def load(path: str, legacy_gas_tags: bool = False) -> Scenario:
+    """Read and prepare a scenario file; raises ScenarioError where the
+    reference reports an error.  legacy_gas_tags also reads the gas density
+    written as <GasDensityFunction index=..><VolumeDensity value unit/>
+    (the form the reference's own scenario files use, which its reader
+    ignores) as the DensityFunction."""
     try:
         root = ET.parse(path).getroot()
     except ET.ParseError as e:
@@ -544,10 +625,7 @@ def load(path: str) -> Scenario:
     next_id = 0
     for g, bg in enumerate(bgl.findall("BodyGroup")):
         ga = _attrs(bg, ("description", "epoch", "offset", "referenceframe", "guid"))
-        if "epoch" in ga:
-            raise ScenarioError("body groups with an epoch are not supported")
-        if "offset" in ga and _double(ga, "offset", bg) != 0.0:
-            raise ScenarioError("body groups with an offset are not supported")
+        offset = _double(ga, "offset", bg) if "offset" in ga else 0.0
         items = bg.find("Items")
         if items is None:
             raise ScenarioError("Missing Items tag")
@@ -557,7 +635,8 @@ def load(path: str) -> Scenario:
             next_id += 1
         if not bodies:
             raise ScenarioError("Missing Body tag")
-        groups.append((ga.get("referenceframe", ""), bodies))
+        groups.append(BodyGroup(ga.get("description", "").strip(), ga.get("epoch", "").strip(), offset,
+                                ga.get("referenceframe", "").strip(), bodies))
     if not groups:
         raise ScenarioError("Missing BodyGroup tag")
     gas = None
@@ -567,12 +646,20 @@ def load(path: str) -> Scenario:
         if na.get("fargopath"):
             raise ScenarioError("FARGO coupling is not supported")
         gc = neb.find("GasComponent")
-        gas = _read_gas(gc) if gc is not None else scenarios.default_gas()
-    bodies, insertion = _check_and_prepare(st, groups)
-    system = _to_system(st, bodies, gas)
+        gas = _read_gas(gc, legacy_gas_tags) if gc is not None else scenarios.default_gas()
+    _check_body_group_list(groups)
+    groups, time0, n_distinct = _initialize(st, groups)
+    body_list, insertion = [], []
+    for g in insertion_order(st, groups, time0, n_distinct):
+        body_list, written = insert_group(body_list, g.bodies)
+        insertion += [b.id for b in written]
+    check_type_order(body_list)
+    system = build_system(st, body_list, gas)
+    st.h0 = first_step(body_list, st.length)
+    system.h0 = st.h0
     return Scenario(name=sa.get("name", ""), description=sa.get("description", ""),
-                    directory=os.path.dirname(os.path.abspath(path)), settings=st, bodies=bodies, system=system,
-                    insertion=insertion)
+                    directory=os.path.dirname(os.path.abspath(path)), settings=st, bodies=body_list, system=system,
+                    insertion=insertion, groups=groups, time0=time0, n_distinct_start_times=n_distinct, gas=gas)
 
 
 def _calculate_phase(mu: float, el: list) -> list:
@@ -609,29 +696,53 @@ def _calculate_phase(mu: float, el: list) -> list:
     return [kszi * P[k] + eta * Q[k] for k in range(3)] + [vk * P[k] + ve * Q[k] for k in range(3)]
 
 
-def _check_and_prepare(st: Settings, groups: list) -> list:
-    # Simulation::CheckBodyGroupList (Simulation.cpp:174-220)
-    if len(groups) == 1 and len(groups[0][1]) <= 1:
+def _check_body_group_list(groups: list):
+    """Simulation::CheckBodyGroupList (Simulation.cpp:174-220)."""
+    if len(groups) == 1 and len(groups[0].bodies) <= 1:
         raise ScenarioError("There is only one body defined in the Simulation!")
-    all_bodies = [b for _, bs in groups for b in bs]
+    all_bodies = [b for g in groups for b in g.bodies]
     n_cb = sum(1 for b in all_bodies if b.type == abi.CENTRAL_BODY)
     if n_cb > 1:
         raise ScenarioError("There are more than 1 central body defined!")
     if n_cb == 0:
         raise ScenarioError("The central body is not defined!")
-    if len({rf for rf, _ in groups if rf}) > 1:
+    if len({g.reference_frame for g in groups if g.reference_frame}) > 1:
         raise ScenarioError("The BodyGroups have different reference frames!")
-    # Simulation::SetTimeAndSaveOfTimeLine: a group with massive bodies must exist
-    if not any(b.type not in (abi.CENTRAL_BODY, abi.TEST_PARTICLE) and b.mass > 0 for b in all_bodies):
-        raise ScenarioError("None of the BodyGroups contains massive bodies!")
-    # the groups' start times are all 0: the sort is stable, a backward run reverses the list
-    ordered_groups = [bs for _, bs in groups]
-    if st.length < 0:
-        ordered_groups.reverse()
-    central = next(b for b in all_bodies if b.type == abi.CENTRAL_BODY)
+
+
+def _initialize(st: Settings, groups: list):
+    """Simulation::Initialize (Simulation.cpp:28-172): start times from the
+    epochs, the groups ordered by start time, the time line's time, phases
+    and radii.  Returns the ordered groups, the time line's time and the
+    number of distinct start times."""
+    forward = st.length >= 0
+    if not st.start_defined:  # SetStartTimeOfMainPhase: the last (forward) or first epoch, else 0
+        jds = sorted({julian_date(g.epoch) for g in groups if g.epoch})
+        st.start = (jds[-1] if forward else jds[0]) if jds else 0.0
+    for g in groups:  # BodyGroup::SetStartTime
+        g.start_time = (julian_date(g.epoch) if g.epoch else st.start) + g.offset
+    distinct = sorted({g.start_time for g in groups})
+    count = 0  # BodyGroupList::DistinctStartTimesOfMassiveBodies: non-central bodies with characteristics
+    for t in distinct:
+        count += sum(1 for g in groups if g.start_time == t for b in g.bodies
+                     if b.type not in (abi.TEST_PARTICLE, abi.CENTRAL_BODY)) > 0
+    if not st.enable_distinct_start_times and count > 1:
+        raise ScenarioError("More than 1 BodyGroup contain massive bodies with different start times!")
+    groups = sorted(groups, key=lambda g: g.start_time)  # std::list::sort is stable
+    if not forward:
+        groups.reverse()
+    if not st.enable_distinct_start_times:  # SetTimeAndSaveOfTimeLine
+        massive = [g for g in groups
+                   if any(b.type not in (abi.CENTRAL_BODY, abi.TEST_PARTICLE) and b.mass > 0 for b in g.bodies)]
+        if not massive:
+            raise ScenarioError("None of the BodyGroups contains massive bodies!")
+        time0 = massive[0].start_time
+    else:
+        time0 = groups[0].start_time
+    central = next(b for g in groups for b in g.bodies if b.type == abi.CENTRAL_BODY)
     central_gm = GAUSS2 * central.mass
-    for bs in ordered_groups:  # Simulation::SetPhasesRadiiDensity (:131-172)
-        for b in bs:
+    for g in groups:  # Simulation::SetPhasesRadiiDensity (:131-172)
+        for b in g.bodies:
             if b.type != abi.CENTRAL_BODY and b.phase is None:
                 mu = central_gm + (GAUSS2 * b.mass if b.type != abi.TEST_PARTICLE else 0.0)
                 b.phase = _calculate_phase(mu, b.elements)
@@ -643,31 +754,65 @@ def _check_and_prepare(st: Settings, groups: list) -> list:
                 b.radius = math.pow(3.0 / (4.0 * PI) * b.mass / b.density, 1.0 / 3.0)
             else:                # Characteristics::CalculateDensity / CalculateVolume
                 b.density = b.mass / (4.0 / 3.0 * PI * math.pow(b.radius, 3))
-    # Simulator::PopulateBodyList / Insert / SetIteratorAfter (Simulator.cpp:449-508)
-    body_list, insertion = [], []
-    for bs in ordered_groups:
-        it = 0
-        for t in range(1, 8):
-            of_type = [b for b in bs if b.type == t]
-            if not of_type:
-                continue
-            insertion += [b.id for b in of_type]
-            while it < len(body_list) and body_list[it].type != t:
-                it += 1
-            while it < len(body_list) and body_list[it].type == t:
-                it += 1
-            body_list[it:it] = of_type
-            it += len(of_type)  # std::list::insert leaves the iterator after the inserted range
-    if any(body_list[k].type > body_list[k + 1].type for k in range(len(body_list) - 1)):
+    return groups, time0, len(distinct)
+
+
+def sync_start_times(st: Settings, groups: list, time0: float) -> list:
+    """The start times Simulator::Synchronization (Simulator.cpp:322-390) walks:
+    the distinct start times in the run's direction, preceded by the time
+    line's time unless distinct start times are enabled."""
+    times = sorted({g.start_time for g in groups})
+    if st.length < 0:
+        times.reverse()
+    if not st.enable_distinct_start_times:
+        times.insert(0, time0)
+    return times
+
+
+def insertion_order(st: Settings, groups: list, time0: float, n_distinct: int) -> list:
+    """The groups in the order the run inserts them: by the synchronisation's
+    start times when there are several, else in the list's order
+    (Simulator::PopulateBodyList)."""
+    if n_distinct <= 1:
+        return list(groups)
+    out = []
+    for t in sync_start_times(st, groups, time0):
+        out += [g for g in groups if g.start_time == t and g not in out]
+    return out
+
+
+def insert_group(body_list: list, group_bodies: list):
+    """Simulator::Insert / SetIteratorAfter (Simulator.cpp:449-495): each type
+    of the group, in type order, goes after the bodies of that type found from
+    the position the previous type left.  Returns the new list and the
+    group's bodies in the order their properties are written."""
+    body_list = list(body_list)
+    written = []
+    it = 0
+    for t in range(1, 8):
+        of_type = [b for b in group_bodies if b.type == t]
+        if not of_type:
+            continue
+        written += of_type
+        while it < len(body_list) and body_list[it].type != t:
+            it += 1
+        while it < len(body_list) and body_list[it].type == t:
+            it += 1
+        body_list[it:it] = of_type
+        it += len(of_type)  # std::list::insert leaves the iterator after the inserted range
+    return body_list, written
+
+
+def check_type_order(body_list: list):
+    if (not body_list or body_list[0].type != abi.CENTRAL_BODY
+            or any(body_list[k].type > body_list[k + 1].type for k in range(len(body_list) - 1))):
         raise ScenarioError("the body groups would be integrated out of type order (central body first, then "
                             "giant, rocky and proto-planets, super-planetesimals, planetesimals, test particles)")
-    return body_list, insertion
 
 
-def _to_system(st: Settings, bodies: list, gas: dict | None) -> scenarios.System:
-    """Simulator::BodyListToBodyData (Simulator.cpp:525-593), the phases moved
-    to the barycentre in a barycentric run, and the first step of
-    Simulator::MainIntegration (:431-435), from the heliocentric phases."""
+def build_system(st: Settings, bodies: list, gas: dict | None) -> scenarios.System:
+    """Simulator::BodyListToBodyData (Simulator.cpp:525-593): the body data of
+    the current body list, moved to the barycentre in a barycentric run."""
     n = len(bodies)
     counts = tuple(sum(1 for b in bodies if b.type == t) for t in range(1, 8))
     ge, gs = np.zeros(n), np.zeros(n)
@@ -693,22 +838,20 @@ def _to_system(st: Settings, bodies: list, gas: dict | None) -> scenarios.System
         for i in range(n):
             for j in range(6):
                 y0[6 * i + j] -= bc[j]
-    system = scenarios.System(
+    return scenarios.System(
         name="scenario", counts=counts, id=np.array([b.id for b in bodies], np.int32),
         type=np.array([b.type for b in bodies], np.int32),
         mig_type=np.array([b.mig_type for b in bodies], np.int32),
         mig_stop_at=np.array([b.mig_stop_at for b in bodies]), mass=mass, radius=radius, density=density, cd=cd,
-        gamma_stokes=gs, gamma_epstein=ge, y0=y0, gas=gas,
-        barycentric=st.barycentric, integrator=st.integrator, length=st.length)
-    st.h0 = first_step(bodies, st.length)
-    system.h0 = st.h0
-    return system
+        gamma_stokes=gs, gamma_epstein=ge, y0=y0, gas=gas, barycentric=st.barycentric, integrator=st.integrator,
+        length=st.length)
 
 
-def first_step(bodies: list, length: float) -> float:
+def first_step(bodies: list, length: float, divisor: float = 50000.0) -> float:
     """Simulator::ShortestPeriod (Simulator.cpp:510-523) with
-    Body::CalculateOrbitalPeriod (Body.cpp:89-98) over the phases, / 50,000,
-    signed by the direction and clamped to the length."""
+    Body::CalculateOrbitalPeriod (Body.cpp:89-98) over the body list's phases,
+    / 50,000 (the main integration; 50 for synchronisation and
+    pre-integration), signed by the direction and clamped to the length."""
     central_gm = GAUSS2 * bodies[0].mass
     period = 1.0e10
     for b in bodies:
@@ -724,7 +867,7 @@ def first_step(bodies: list, length: float) -> float:
             p = 2.0 * PI * math.sqrt((a * a * a) / mu)
         if 0 < p < period:
             period = p
-    h0 = period / 50000.0 if length >= 0 else -period / 50000.0
+    h0 = period / divisor if length >= 0 else -period / divisor
     if abs(h0) > abs(length):
         h0 = length
     return h0

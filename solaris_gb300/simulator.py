@@ -1,31 +1,42 @@
-"""The reference's main integration of a scenario file on the device:
-Simulator::MainIntegration, Integrate, DecisionMaking and CheckEvent
-(Solaris/Simulator.cpp:121-250, :423-447, :621-735) with the output files of
-Solaris/BinaryFileAdapter.cpp.
+"""The reference's simulation of a scenario file on the device:
+Simulator::Run with its synchronisation of body groups that start at
+different epochs, the pre-integration to a TimeLine start and the main
+integration (Solaris/Simulator.cpp:62-447), each an Integrate /
+DecisionMaking / CheckEvent loop (:121-250, :621-735), with the output files
+of Solaris/BinaryFileAdapter.cpp.
 
 Per accepted step, as the reference does it: one integrator Driver call on
 the device, then the events (ejection, hit-centrum, collisions) applied on
-the device, the stop test, the step clamped to the end of the run, a
+the device, the stop test, the step clamped to the end of the phase, a
 phases + integrals record when the output interval is full, the step clamped
-to the next output time; every 100 steps coordinates below 1e-50 are set to
-zero (Tools::CheckAgainstSmallestNumber).  Phases and integrals records are
-written in the reference's binary layouts by the output writer thread;
-TwoBodyAffair records, the constant / variable / composition property
-records of body insertion and of every merge, and the log lines are written
-here on the host.
+to the next output time; every 100 steps (counted over the whole run)
+coordinates below 1e-50 are set to zero (Tools::CheckAgainstSmallestNumber).
+Phases and integrals records are written in the reference's binary layouts
+by the output writer thread; TwoBodyAffair records, the constant / variable
+/ composition property records of body insertion and of every merge, and the
+log lines are written here on the host, which keeps the reference's body
+list (the characteristics it replays with the reference's arithmetic, the
+phases it takes back from the device after every phase).
+
+The end test: the reference compares the absolute time with the phase's
+length (DecisionMaking, :197-219), so a run that starts at an epoch's Julian
+date stops as soon as |time| >= |length|, after one step for dates beyond the
+length; relative_end_test=True measures the time integrated in the phase
+instead, as the reference's unused second DecisionMaking (:252-320) does.
 
 A collision's TwoBodyAffair record carries, as the reference writes it
 (Simulator.cpp:709), the phases of the step's starting state at the
 survivor's and the merger's current indices (bodyData.y after the swap);
 that state is read back before each step of a run with collisions.
 
-A backend object does the numerical work: EngineBackend is the device
-context; any object with the same methods (step, events, n_total, state,
-zero_below_smallest, save_phases, save_integrals, close) can stand in for
-it.
+A backend does the numerical work of one Integrate call: EngineBackend is a
+device context; any factory (system, settings, directory) -> object with
+the same methods (step, events, n_total, state, zero_below_smallest,
+save_phases, save_integrals, close) can stand in for it.
 """
 from __future__ import annotations
 
+import dataclasses
 import math
 import os
 import struct
@@ -34,6 +45,7 @@ import time as _time
 import numpy as np
 
 from . import abi, engine
+from . import scenario_xml as sx
 from .scenario_xml import BodySpec, Component, Scenario, ScenarioError, YEAR_TO_DAY, PI
 
 SMALLEST_NUMBER = 1.0e-50
@@ -44,10 +56,9 @@ EJECTION, HIT_CENTRUM, COLLISION = 0, 1, 3
 class EngineBackend:
     """A device context driven one accepted step at a time."""
 
-    def __init__(self, scenario: Scenario, directory: str, device: int = 0, precision: int = abi.PRECISION_FP64):
-        st = scenario.settings
-        self.ctx = engine.Context(scenario.system, device=device, precision=precision)
-        self.ctx.set_state(scenario.system.y0)
+    def __init__(self, system, st, directory: str, device: int = 0, precision: int = abi.PRECISION_FP64):
+        self.ctx = engine.Context(system, device=device, precision=precision)
+        self.ctx.set_state(system.y0)
         self.integrator = st.integrator
         self.out = engine.Output(self.ctx, os.path.join(directory, st.phases), os.path.join(directory, st.integrals))
         self.tl = abi.SolTimeLine(0.0, 0.0, 0.0)
@@ -106,15 +117,38 @@ def _short_string(s: str) -> bytes:
 
 
 class _Body:
-    """The host's copy of a body's characteristics (the reference's Body list)."""
+    """The host's copy of a body (the reference's Body list entry): its
+    characteristics, replayed through merges, and its phase, taken back from
+    the device after every phase."""
 
     def __init__(self, spec: BodySpec):
         self.spec = spec
+        self.id = spec.id
         self.type = spec.type
+        self.mig_type = spec.mig_type
+        self.mig_stop_at = spec.mig_stop_at
+        self.cd = spec.cd
         self.mass = spec.mass if spec.type != abi.TEST_PARTICLE else 0.0
         self.radius = spec.radius if spec.type != abi.TEST_PARTICLE else 0.0
         self.density = spec.density if spec.type != abi.TEST_PARTICLE else 0.0
         self.components = [Component(c.name, c.ratio) for c in spec.components]
+        self.phase = list(spec.phase)
+
+
+@dataclasses.dataclass
+class TimeLine:
+    """Solaris/TimeLine.h: one phase's time line."""
+    time: float
+    length: float
+    output: float
+    h_next: float = 0.0
+    h_did: float = 0.0
+    elapsed: float = 0.0
+    last_save: float = 0.0
+    save: float = 0.0
+
+    def forward(self) -> bool:
+        return self.length >= 0
 
 
 class _Properties:
@@ -200,21 +234,26 @@ def _yr(days: float) -> str:
 
 
 class Simulator:
-    """Runs a scenario's main integration and writes the reference's output
-    files into `directory` (the scenario file's directory by default)."""
+    """Runs a scenario (synchronisation, pre-integration, main integration)
+    and writes the reference's output files into `directory` (the scenario
+    file's directory by default)."""
 
     def __init__(self, scenario: Scenario, directory: str | None = None, backend=None, device: int = 0,
-                 precision: int = abi.PRECISION_FP64):
+                 precision: int = abi.PRECISION_FP64, relative_end_test: bool = False):
         self.sc = scenario
         self.dir = directory or scenario.directory
         os.makedirs(self.dir, exist_ok=True)
-        self.backend = backend if backend is not None else EngineBackend(scenario, self.dir, device, precision)
-        self.bodies = {b.id: _Body(b) for b in scenario.bodies}
-        self.order = [b.id for b in scenario.bodies]  # ids by index, as the device compacts them
+        self.factory = backend if backend is not None else (
+            lambda system, st, d: EngineBackend(system, st, d, device, precision))
+        self.relative_end_test = relative_end_test
+        self.bodies = {b.id: _Body(b) for g in scenario.groups for b in g.bodies}
+        self.body_list = []  # the bodies being integrated, in the device's order
         self.props = _Properties(self.dir, scenario.settings)
         self.event_id = 0
-        self.steps = 0
+        self.steps = 0      # Counter::succededStep, over the whole run
+        self.phases = 0
         self.affairs = []
+        self.be = None
 
     # -- log (BinaryFileAdapter::Log) ----------------------------------------------------
     def _log(self, msg: str):
@@ -222,14 +261,18 @@ class Simulator:
         with open(os.path.join(self.dir, self.sc.settings.log), "a") as f:
             f.write(f"{stamp} {msg}\n")
 
-    # -- body insertion (Simulator::Insert writes the properties of each type group) --------
-    def _insert_records(self, time: float):
+    # -- Simulator::Insert: a group joins the body list; its properties are written ----------
+    def _insert(self, group, time: float):
+        self.body_list, written = sx.insert_group(self.body_list, [self.bodies[b.id] for b in group.bodies])
         const, var, comp = [], [], []
-        for bid in self.sc.insertion:
-            b = self.bodies[bid]
+        for b in written:
             const.append(self.props.constant(b))
             var.append(self.props.variable(b, time, comp))
         self.props.append(const, var, comp)
+
+    def _populate(self, time: float):
+        for g in self.sc.groups:
+            self._insert(g, time)
 
     # -- CheckEvent ------------------------------------------------------------------------
     def _check_event(self, time: float, y_start):
@@ -237,7 +280,7 @@ class Simulator:
         factor = st.collision if st.collision is not None else 0.0
         if st.ejection <= 0.0 and st.hit_centrum <= 0.0 and factor <= 0.0:
             return
-        affairs = self.backend.events(time, st.ejection, st.hit_centrum, factor)
+        affairs = self.be.events(time, st.ejection, st.hit_centrum, factor)
         if not affairs:
             return
         # TwoBodyAffair ids: ejections and hit-centrum bodies are numbered in body
@@ -282,60 +325,131 @@ class Simulator:
             else:
                 self._log(f"Collision: At {_yr(a['time'])} [yr] between body with id: {a['id1']} "
                           f"and id: {a['id2']}")
-            self._remove(a["id2"] if a["type"] == HIT_CENTRUM else m.spec.id)
+            self._remove(a["id2"] if a["type"] == HIT_CENTRUM else m.id)
         if var:
             self.props.append([], var, comp)
 
     def _remove(self, bid: int):
-        if bid in self.order:
-            self.order.remove(bid)
+        self.body_list = [b for b in self.body_list if b.id != bid]
 
-    # -- MainIntegration / Integrate / DecisionMaking ------------------------------------
-    def run(self) -> dict:
+    # -- Integrate / DecisionMaking ---------------------------------------------------------
+    def _integrate(self, tl: TimeLine):
         st = self.sc.settings
-        be = self.backend
-        if st.length == 0.0:  # Simulator::Run integrates only a non-zero length
-            be.close()
-            return dict(steps=0, time=0.0, affairs=[], seconds=0.0)
-        self._insert_records(0.0)
-        t = 0.0
-        h_next = st.h0
-        last_save = 0.0
-        be.save_phases(t)
-        be.save_integrals(t)
-        t_wall = _time.time()
+        sx.check_type_order(self.body_list)
+        system = sx.build_system(st, self.body_list, self.sc.gas)
+        self.be = be = self.factory(system, st, self.dir)
+        self.phases += 1
         collisions = st.collision is not None
-        while True:
-            y_start = be.state() if collisions else None
-            t, h_did, h_next = be.step(t, h_next)
-            self.steps += 1
-            # DecisionMaking (Simulator.cpp:181-250)
-            last_save += h_did
-            actual = t  # 1000 YearToDay millenium + time, the millenium counter stays 0
-            self._check_event(t, y_start)
-            stop = False
-            if abs(actual) >= abs(st.length):
-                stop = True
-            elif be.n_total() <= 1:
-                self._log("The total number of bodies reduced to 1!")
-                stop = True
-            else:
-                if abs(actual + h_next) > abs(st.length):
-                    h_next = st.length - actual
-                if abs(last_save) >= abs(st.output):
-                    be.save_phases(t)
-                    be.save_integrals(t)
-                    last_save = 0.0
-                if abs(last_save + h_next) > abs(st.output):
-                    h_next = st.output - last_save
-            if self.steps % CHECK_FOR_SMALLEST == 0:
-                be.zero_below_smallest()
-            if stop:
+        sum_all = sum_save = 0.0  # the phase-relative clock of relative_end_test
+        try:
+            be.save_phases(tl.time)
+            be.save_integrals(tl.time)
+            while True:
+                y_start = be.state() if collisions else None
+                tl.time, tl.h_did, tl.h_next = be.step(tl.time, tl.h_next)
+                self.steps += 1
+                tl.elapsed += tl.h_did
+                tl.last_save += tl.h_did
+                sum_all += tl.h_did
+                sum_save += tl.h_did
+                self._check_event(tl.time, y_start)
+                clock = sum_all if self.relative_end_test else tl.time  # 1000 YearToDay millenium + time
+                since = sum_save if self.relative_end_test else tl.last_save
+                stop = False
+                if abs(clock) >= abs(tl.length):
+                    stop = True
+                elif be.n_total() <= 1:
+                    self._log("The total number of bodies reduced to 1!")
+                    stop = True
+                else:
+                    if abs(clock + tl.h_next) > abs(tl.length):
+                        tl.h_next = tl.length - clock
+                    if abs(since) >= abs(tl.output):
+                        be.save_phases(tl.time)
+                        be.save_integrals(tl.time)
+                        tl.last_save = sum_save = since = 0.0
+                        if self.relative_end_test:
+                            tl.save += tl.output
+                    if abs(since + tl.h_next) > abs(tl.output):
+                        tl.h_next = tl.output - since
+                if self.steps % CHECK_FOR_SMALLEST == 0:
+                    be.zero_below_smallest()
+                if stop:
+                    break
+            # UpdateBodyListAfterIntegration: the phases go back to the body list
+            y = be.state()
+            for k, b in enumerate(self.body_list):
+                b.phase = [float(v) for v in y[6 * k:6 * k + 6]]
+            be.save_phases(tl.time)
+            be.save_integrals(tl.time)
+        finally:
+            be.close()
+            self.be = None
+
+    # -- Simulator::Run ------------------------------------------------------------------------
+    def _synchronization(self, main: TimeLine):
+        """Simulator::Synchronization (Simulator.cpp:322-390)."""
+        st, sc = self.sc.settings, self.sc
+        sync = dataclasses.replace(main)
+        times = sx.sync_start_times(st, sc.groups, sc.time0)
+        inserted = set()
+        for k, t in enumerate(times):
+            for g in sc.groups:
+                if g.start_time == t and id(g) not in inserted:
+                    self._insert(g, sync.time)
+                    inserted.add(id(g))
+                    self._log(f"The bodygroup ({g.description}) with epoch: {g.epoch} was included")
+            if k + 1 >= len(times):
                 break
-        be.save_phases(t)
-        be.save_integrals(t)
-        be.close()
-        return dict(steps=self.steps, time=t, affairs=self.affairs, seconds=_time.time() - t_wall)
+            sync.length = times[k + 1] - sync.time
+            sync.output = main.output if sync.forward() else -main.output
+            if sync.length != 0.0 and len(self.body_list) > 1:
+                sx.check_type_order(self.body_list)
+                sync.h_did = 0.0
+                sync.h_next = sx.first_step(self.body_list, sync.length, 50.0)
+                self._integrate(sync)
+        main.time = sync.time
+        main.save = sync.time
+
+    def _pre_integration(self, main: TimeLine):
+        """Simulator::PreIntegration (Simulator.cpp:392-421).  The reference
+        takes the shortest period of an empty body list when nothing was
+        synchronised; here the list is populated first."""
+        st = self.sc.settings
+        pre = dataclasses.replace(main)
+        pre.length = st.start - pre.time
+        pre.output = main.output if pre.forward() else -main.output
+        pre.h_did = 0.0
+        if not self.body_list:
+            self._populate(pre.time)
+        sx.check_type_order(self.body_list)
+        pre.h_next = sx.first_step(self.body_list, pre.length, 50.0)
+        self._integrate(pre)
+
+    def _main_integration(self, main: TimeLine):
+        """Simulator::MainIntegration (Simulator.cpp:423-447)."""
+        if not self.body_list:
+            self._populate(main.time)
+        sx.check_type_order(self.body_list)
+        main.h_did = 0.0
+        main.h_next = sx.first_step(self.body_list, main.length, 50000.0)
+        self._integrate(main)
+
+    def run(self) -> dict:
+        st, sc = self.sc.settings, self.sc
+        t_wall = _time.time()
+        main = TimeLine(time=sc.time0, length=st.length, output=st.output, save=sc.time0)
+        if sc.n_distinct_start_times > 1:
+            self._log("The synchronization phase of the simulation begins")
+            self._synchronization(main)
+        if st.start_defined:
+            self._log("The pre-integration phase of the simulation begins")
+            self._pre_integration(main)
+        if st.length != 0.0:
+            self._log("The main-integration phase of the simulation begins")
+            self._main_integration(main)
+        return dict(steps=self.steps, phases=self.phases, time=main.time, affairs=self.affairs,
+                    seconds=_time.time() - t_wall)
 
 
 def run_file(path: str, directory: str | None = None, device: int = 0, precision: int = abi.PRECISION_FP64) -> dict:

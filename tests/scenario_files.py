@@ -9,7 +9,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SCENARIOS = os.path.join(HERE, "golden", "scenarios")
-NAMES = ("ejection_rkf78", "gas_rk4", "bary_dopri", "collision_rkf78")
+NAMES = ("ejection_rkf78", "gas_rk4", "bary_dopri", "collision_rkf78", "epochs_rkf78", "pre_dopri")
 
 
 def xml_path(name: str) -> str:

@@ -38,8 +38,8 @@ def test_scenario_files_match_the_reference_program(tmp_path, name):
     property files of the oracle-driven run are the reference program's bytes."""
     sc = sx.load(xml_path(name))
     out = str(tmp_path)
-    r = sim.Simulator(sc, directory=out, backend=oracle.ScenarioBackend(sc, out)).run()
-    assert r["steps"] > 100
+    r = sim.Simulator(sc, directory=out, backend=oracle.ScenarioBackend).run()
+    assert r["steps"] > 40
     gold = golden_dir(name)
     expected = sorted(os.listdir(gold))
     produced = sorted(f for f in os.listdir(out) if f != sc.settings.log)
@@ -52,6 +52,7 @@ def test_scenario_files_match_the_reference_program(tmp_path, name):
         assert got == want, fn
     if name in ("ejection_rkf78", "gas_rk4", "collision_rkf78"):
         assert len(r["affairs"]) == 1
+    assert r["phases"] == {"epochs_rkf78": 3, "pre_dopri": 3}.get(name, 1)
 
 
 def test_initial_state_is_the_reference_programs():
@@ -59,6 +60,8 @@ def test_initial_state_is_the_reference_programs():
     state: ids, insertion order, units, Kepler phases, barycentric shift."""
     for name in NAMES:
         sc = sx.load(xml_path(name))
+        if sc.n_distinct_start_times > 1 or sc.settings.start_defined:
+            continue  # the first record is the first synchronisation phase's
         ph = [f for f in os.listdir(golden_dir(name)) if f.endswith("Phases.dat")][0]
         t, ids, y = read_phases(os.path.join(golden_dir(name), ph))[0]
         assert t == 0.0
@@ -168,7 +171,6 @@ def test_barycentric_shift(tmp_path):
     ([[STAR, planet(kind="testparticle")]], {}, "massive bodies"),
     ([[STAR, planet()]], {"integ": "euler"}, "Unknown integrator"),
     ([[STAR, planet()]], {"length": "0"}, "length"),
-    ([[STAR, planet()]], {"sattr": ' enableDistinctStartTimes="true"'}, "distinct start times"),
     ([[STAR, planet()]], {"sattr": ' color="red"'}, "Unknown attribute"),
     ([[STAR, planet()]], {"extra": '<Collision factor="0.5"/>'}, "factor"),
     ([[STAR, planet(chars='<Mass value="1"/><Radius value="1"/><Density value="1"/>')]], {}, "radius and the density"),
@@ -186,17 +188,100 @@ def test_reader_errors(tmp_path, groups, kw, message):
         sx.load(write(tmp_path, groups, **kw))
 
 
-def test_refused_phases(tmp_path):
-    p = tmp_path / "e.xml"
-    p.write_text('<Simulation><Settings><Integrator/><TimeLine length="1" start="5"/></Settings>'
-                 f'<BodyGroupList><BodyGroup><Items>{STAR}{planet()}</Items></BodyGroup></BodyGroupList></Simulation>')
-    with pytest.raises(sx.ScenarioError, match="pre-integration"):
+def test_julian_dates():
+    """Ephemeris::GetJulianDate: Julian dates, dates and packed dates at 0h UT."""
+    assert sx.julian_date("JD2451545.0") == 2451545.0 and sx.julian_date("jd10") == 10.0
+    assert sx.julian_date("20000101") == 2451544.5
+    assert sx.julian_date("19991231") == 2451543.5
+    assert sx.julian_date("K0111") == 2451910.5      # 2001-01-01
+    assert sx.julian_date("J961A") == sx.julian_date("19960110")
+    assert sx.julian_date("15821004") - sx.julian_date("15821015") == -1.0  # the Gregorian reform
+    for bad in ("JD24x", "123456789", "L0101", "K01D1", "K01", "x"):
+        with pytest.raises(sx.ScenarioError, match="format"):
+            sx.julian_date(bad)
+
+
+def _epoch_xml(tmp_path, epochs, extra_settings="", timeline='length="2" output="0.5" unit="year"', name="ep.xml"):
+    groups = [[STAR, planet(name="G", a=5.0), planet(kind="rockyplanet", name="R", a=1.0,
+                                                     chars='<Mass value="1" unit="earth"/>')],
+              [planet(kind="testparticle", name="T", a=2.0), planet(kind="testparticle", name="U", a=3.0, M=2.0)]]
+    g = "".join(f'<BodyGroup epoch="{e}"><Items>{"".join(bs)}</Items></BodyGroup>' if e else
+                f'<BodyGroup><Items>{"".join(bs)}</Items></BodyGroup>' for e, bs in zip(epochs, groups))
+    p = tmp_path / name
+    p.write_text(f'<Simulation><Settings{extra_settings}><Integrator/><TimeLine {timeline}/></Settings>'
+                 f'<BodyGroupList>{g}</BodyGroupList></Simulation>')
+    return str(p)
+
+
+def test_start_times(tmp_path):
+    sc = sx.load(_epoch_xml(tmp_path, ["JD100", "JD40"]))
+    assert sc.time0 == 100.0 and sc.n_distinct_start_times == 2 and sc.settings.start == 100.0
+    assert [g.start_time for g in sc.groups] == [40.0, 100.0]
+    assert sx.sync_start_times(sc.settings, sc.groups, sc.time0) == [100.0, 40.0, 100.0]
+    sc = sx.load(_epoch_xml(tmp_path, ["JD100", ""]))  # a group without epoch starts at the last epoch
+    assert sc.n_distinct_start_times == 1 and sc.time0 == 100.0
+    with pytest.raises(sx.ScenarioError, match="different start times"):
+        p = tmp_path / "two.xml"
+        p.write_text('<Simulation><Settings><Integrator/><TimeLine length="1"/></Settings><BodyGroupList>'
+                     f'<BodyGroup epoch="JD1"><Items>{STAR}{planet()}</Items></BodyGroup>'
+                     f'<BodyGroup epoch="JD2"><Items>{planet(name="Q", a=7.0)}</Items></BodyGroup>'
+                     '</BodyGroupList></Simulation>')
         sx.load(str(p))
-    p.write_text('<Simulation><Settings><Integrator/><TimeLine length="1"/></Settings>'
-                 f'<BodyGroupList><BodyGroup epoch="2451545.0"><Items>{STAR}{planet()}</Items></BodyGroup>'
-                 '</BodyGroupList></Simulation>')
-    with pytest.raises(sx.ScenarioError, match="epoch"):
-        sx.load(str(p))
+
+
+def test_relative_end_test_shifts_a_run_in_time(tmp_path):
+    """With the phase-relative end test, a run whose groups share an epoch is
+    the run without epochs moved in time: the same steps and phases."""
+    out = []
+    for k, epochs in enumerate((["", ""], ["JD2451545.0", "JD2451545.0"])):
+        sc = sx.load(_epoch_xml(tmp_path, epochs, name=f"e{k}.xml"))
+        d = tmp_path / f"o{k}"
+        r = sim.Simulator(sc, directory=str(d), backend=oracle.ScenarioBackend, relative_end_test=True).run()
+        out.append((r, read_phases(str(d / "Phases.dat"))))
+    (r0, p0), (r1, p1) = out
+    assert r0["steps"] == r1["steps"] > 50 and len(p0) == len(p1) == 5
+    for (t0, i0, y0), (t1, i1, y1) in zip(p0, p1):
+        assert np.array_equal(i0, i1) and np.array_equal(y0, y1)
+        assert abs((t1 - 2451545.0) - t0) <= 1e-6
+    # the reference's end test compares the absolute time: the same epoch run stops after one step
+    sc = sx.load(_epoch_xml(tmp_path, ["JD2451545.0", "JD2451545.0"], name="e2.xml"))
+    r = sim.Simulator(sc, directory=str(tmp_path / "o2"), backend=oracle.ScenarioBackend).run()
+    assert r["steps"] == 1
+
+
+def test_synchronisation_integrates_the_groups_to_a_common_time(tmp_path):
+    """relative_end_test: the planets are integrated back from their epoch to
+    the test particles' epoch, the particles join, and both go forward."""
+    sc = sx.load(_epoch_xml(tmp_path, ["JD100", "JD40"]))
+    r = sim.Simulator(sc, directory=str(tmp_path / "o"), backend=oracle.ScenarioBackend,
+                      relative_end_test=True).run()
+    recs = read_phases(str(tmp_path / "o" / "Phases.dat"))
+    times = [t for t, _, _ in recs]
+    assert r["phases"] == 3
+    assert times[0] == 100.0 and abs(times[1] - 40.0) <= 1e-9       # back to the particles' epoch
+    assert abs(times[3] - 100.0) <= 1e-9 and len(recs[3][1]) == 5  # forward to the planets' epoch, all bodies
+    assert abs(times[-1] - (100.0 + 2 * 365.25)) <= 1e-9
+
+
+def test_pre_integration_without_synchronisation(tmp_path):
+    """The reference reads the front of an empty body list here (it crashes);
+    the body list is populated first, then pre-integrated to the start."""
+    sc = sx.load(_epoch_xml(tmp_path, ["JD10", "JD10"], timeline='start="30" length="100" output="50" unit="day"'))
+    assert sc.settings.start_defined and sc.n_distinct_start_times == 1
+    r = sim.Simulator(sc, directory=str(tmp_path / "o"), backend=oracle.ScenarioBackend,
+                      relative_end_test=True).run()
+    recs = read_phases(str(tmp_path / "o" / "Phases.dat"))
+    assert r["phases"] == 2 and recs[0][0] == 10.0 and abs(recs[1][0] - 30.0) <= 1e-9
+
+
+def test_legacy_gas_tags(tmp_path):
+    neb = ('<Nebula><GasComponent><GasDensityFunction index="-2.75"><VolumeDensity value="2.8e-9" unit="gcm3"/>'
+           '</GasDensityFunction></GasComponent></Nebula>')
+    p = write(tmp_path, [[STAR, planet()]], nebula=neb)
+    from solaris_gb300 import scenarios
+    assert sx.load(p).system.gas["density"] == scenarios.default_gas()["density"]  # the reference's reader
+    assert sx.load(p, legacy_gas_tags=True).system.gas["density"] == (2.8e-9 * sx.GRAM_PER_CM3_TO_SOLAR_PER_AU3,
+                                                                      -2.75)
 
 
 def test_zero_length_writes_nothing(tmp_path):
@@ -205,7 +290,7 @@ def test_zero_length_writes_nothing(tmp_path):
                  f'<BodyGroupList><BodyGroup><Items>{STAR}{planet()}</Items></BodyGroup></BodyGroupList></Simulation>')
     sc = sx.load(str(p))
     out = tmp_path / "out"
-    r = sim.Simulator(sc, directory=str(out), backend=oracle.ScenarioBackend(sc, str(out))).run()
+    r = sim.Simulator(sc, directory=str(out), backend=oracle.ScenarioBackend).run()
     assert r["steps"] == 0 and os.listdir(out) == []
 
 
