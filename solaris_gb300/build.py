@@ -25,7 +25,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 SOURCES = ["sol_api.cu", "sol_force.cu", "sol_integrate.cu", "sol_diag.cu", "sol_ensemble.cu", "sol_adjoint.cu",
            "sol_terms.cu", "sol_persist.cu",
            "sol_output.cu", "sol_ephem.cu",
-           "sol_events.cu"]
+           "sol_events.cu", "sol_group.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
                      f"-I{INCLUDE}"]

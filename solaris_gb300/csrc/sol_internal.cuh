@@ -191,6 +191,8 @@ struct Rkf78Table {
 const Rkf78Table& sol_rkf78_table();
 int sol_persist_eligible(const sol_ctx* c);
 int sol_persist_rkf78(sol_ctx* c, int n_steps);
+int sol_group_eligible(const sol_ctx* c);
+int sol_group_rkf78(sol_ctx* c, int n_steps);
 int sol_fp64_peak_launch(int device, double* flops);
 
 // ---- PTX helpers: bulk copies (TMA engine) with mbarrier completion --------
