@@ -47,6 +47,12 @@ constexpr int kBlock = 128;       // one warp per SM sub-partition
 constexpr int kMaxSources = 32;   // nm + n_spl
 constexpr int kMaxLocal = 64;     // other bodies per CTA
 constexpr int kMinLocal = 16;
+// Phase-1 work per virtual warp in cycles (measured on the GB300, one warp:
+// pow 5,800, exp 1,100, log10 2,200, sqrt 680, division 430, an FP64 add or
+// multiply 64), for the greedy schedule of the virtual warps onto the warps.
+constexpr int kCostRm3 = 2000, kCostPair = 2000, kCostMig = 30000;
+constexpr int kCostRole0 = 6600, kCostRole1 = 8200, kCostRole2 = 6700, kCostRole3 = 9800;  // the drag's roles
+constexpr int kMaxVw = 3 + 96 + 12 + 3;  // rm3 + pairs + drag roles + migration virtual warps of 96 sinks
 constexpr int kSpreadSmem = 116 * 1024;  // > half of the 228 KB of an SM
 
 __constant__ int g_rk_k[13];
@@ -70,7 +76,7 @@ struct GroupArgs {
   int local;            // other bodies per CTA
   int n_steps;
   // shared-memory layout (offsets in doubles)
-  int o_f, o_y0, o_yt, o_ys, o_yn, o_rm3, o_pp, o_prb, o_xr, o_gm, o_gbuf, o_red, o_mu, o_int;
+  int o_f, o_y0, o_yt, o_ys, o_yn, o_rm3, o_pp, o_prb, o_xr, o_gm, o_gbuf, o_red, o_mu, o_dv, o_int;
 };
 
 __device__ bool group_barrier(const GroupArgs& P, int* s_abort) {
@@ -108,7 +114,10 @@ __device__ bool group_barrier(const GroupArgs& P, int* s_abort) {
 struct Ctl {
   double t, h, h_next, h_did, error_max, eps;
   long long n_acc, n_rej;
-  int status, accepted, abort, npair;
+  int status, accepted, abort, npair, ndrag, nmig;
+  double m0pt, factor;
+  unsigned char sched_n[8];
+  unsigned char sched[8 * kMaxVw];
 };
 
 // Per-CTA view of the shared memory.  Sink slot s < ns is source (body) s,
@@ -132,7 +141,13 @@ struct View {
   int* nsrc;    // [nsink]: sources of the sink (nm + n_spl or nm)
   int* kind;    // [nsink]: gas buffer kind
   int* pair;    // [npair]: sink slot * 32 + source of every (sink, source) pair
-  int nsink, npair;
+  int* dlist;   // [ndrag]: slots of the planetesimals (drag)
+  int* mlist;   // [nmig]: slots of the migrating bodies
+  int nsink, npair, ndrag, nmig;
+  double factor, m0pt;  // ReductionFactor at the step's time, m0^pt
+  const unsigned char* sched;  // [2][4][kMaxVw]: virtual warps of each warp (0: with migration, 1: without)
+  const unsigned char* sched_n;  // [2][4]
+  double* dv;                    // [6][nsink]: the drag's partial results of each planetesimal
 };
 
 // Which gas buffer a body uses (Acceleration::ComputeAstroCentric :176-243):
@@ -153,32 +168,118 @@ __device__ __forceinline__ double* global_gas_buf(const ForceCtx& fc, int i, int
   return fc.mig2 + 3 * (i - c.n_central);
 }
 
-// The buffer part of add_gas_terms: drag evaluated at every evaluation with
-// the drag flag, migration only with its flag and while migType allows it
-// (a migration that reaches its stop sets migType to No).  Out of line: its
-// thousands of instructions inlined into the stage loop evict the hot path
-// from the instruction cache (measured: 3x slower stages without gas).
-__device__ __noinline__ void gas_compute(const ForceCtx& fc, int i, int kind, const double* yi, double t,
-                                            uint32_t flags, double* buf, int* mig) {
+// Migration of one massive body (the migration part of add_gas_terms): only
+// with its flag and while migType allows it (a migration that reaches its
+// stop sets migType to No).  Out of line, like the drag: thousands of
+// instructions inlined into the stage loop evict the hot path from the
+// instruction cache (measured: 3x slower stages).
+__device__ __noinline__ void mig_compute(const ForceCtx& fc, int i, int kind, const double* yi, double factor,
+                                         uint32_t flags, double* buf, int* mig) {
   const GasDev& g = fc.gas;
   const double m0 = fc.mass[0];
   double d[3];
-  if (kind == 1) {
-    if (!(flags & SOL_EVAL_GAS_DRAG)) return;
-    sol_gas_drag(g, sol_reduction_factor(g, t), m0, yi, fc.radius[i], fc.density[i], fc.cd[i], fc.gamma_stokes[i],
-                 fc.gamma_epstein[i], d);
-  } else if (kind == 2) {
+  if (kind == 2) {
     if (!((flags & SOL_EVAL_TYPE_I) && *mig == SOL_MIGRATION_TYPE_I)) return;
-    if (!sol_migration_type1(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
-      *mig = SOL_MIGRATION_NO;
+    if (!sol_migration_type1(g, factor, m0, fc.mass[i], fc.mig_stop_at[i], yi, d)) *mig = SOL_MIGRATION_NO;
   } else {
     if (!((flags & SOL_EVAL_TYPE_II) && *mig == SOL_MIGRATION_TYPE_II)) return;
-    if (!sol_migration_type2(g, sol_reduction_factor(g, t), m0, fc.mass[i], fc.mig_stop_at[i], yi, d))
-      *mig = SOL_MIGRATION_NO;
+    if (!sol_migration_type2(g, factor, m0, fc.mass[i], fc.mig_stop_at[i], yi, d)) *mig = SOL_MIGRATION_NO;
   }
   buf[0] = d[0];
   buf[1] = d[1];
   buf[2] = d[2];
+}
+
+// The regime part of GasDragAC (Acceleration.cpp:364-401) from lambda(r),
+// r, the density's two factors and the gas velocity.
+__device__ __forceinline__ void drag_finish(const GasDev& g, double factor, double m0pt, const double* yi,
+                                           double radius, double density, double cd, double gs, double ge,
+                                           double lambda, double r, double ex, double rp, double vgx, double vgy,
+                                           double out[3]) {
+  const double ux = yi[3] - vgx, uy = yi[4] - vgy, uz = yi[5] - 0.0;
+  const double rho = rp * ex;
+  const double rhoGas = factor * rho;
+  double C;
+  if (radius <= 0.1 * lambda) {
+    // MeanThermalSpeed_CMU(m0, r) -> Temperature_CMU(r, m0) (arguments swapped, :241)
+    const double cT = g.sh_c * g.sh_c * r * g.mmw * g.ctp;
+    const double vth = g.cvth * sqrt(cT * m0pt);
+    C = ge * vth * rhoGas;
+  } else if (radius >= 10.0 * lambda) {
+    const double ul = sqrt(ux * ux + uy * uy + uz * uz);
+    C = gs * ul * rhoGas;
+  } else {
+    const double l1 = 0.1 * lambda, l2 = 10.0 * lambda;
+    const double gE = 1.0 / (density * l1);
+    const double gS = 3.0 / 8.0 * cd / (density * l2);
+    const double cT = g.sh_c * g.sh_c * r * g.mmw * g.ctp;
+    const double vth = g.cvth * sqrt(cT * m0pt);
+    const double ul = sqrt(ux * ux + uy * uy + uz * uz);
+    const double K = gS * ul / (gE * vth);
+    const double eta = l2 / l1;
+    const double kappa = log10(K) / log10(eta);
+    const double gamma = gE * vth * pow(l1, -kappa);
+    C = gamma * pow(radius, kappa) * rhoGas;
+  }
+  out[0] = -C * ux;
+  out[1] = -C * uy;
+  out[2] = -C * uz;
+}
+
+// One of the four independent parts of GasDragAC (Acceleration.cpp:342-363,
+// gas_velocity and gas_density_at of GasComponent.cpp:97-157) for the
+// planetesimal of this lane, in the operations of sol_gas_drag:
+//   role 0: r and the mean free path lambda(r);
+//   role 1: the density's vertical exponential exp(-(z / h(rc))^2);
+//   role 2: the density's power law (or the inner-edge form);
+//   role 3: the gas velocity with its eta(rc) correction.
+// A warp takes one role for 32 planetesimals, so its lanes share the
+// exponent of their pow and run the same instructions; the four roles run in
+// four warps at once and drag_finish combines them.
+__device__ __noinline__ void drag_role(const GasDev& g, int role, double m0, const double* yi, double out[2]) {
+  const double x = yi[0], y = yi[1], z = yi[2];
+  if (role == 0) {
+    const double r = sqrt(x * x + y * y + z * z);
+    out[0] = sol_pl(g.mfp_c, g.mfp_i, r);
+    out[1] = r;
+  } else if (role == 1) {
+    const double rc = sqrt(x * x + y * y);
+    const double hh = sol_pl(g.sh_c, g.sh_i, rc);
+    const double qq = z / hh;
+    out[0] = exp(-(qq * qq));
+  } else if (role == 2) {
+    const double rc = sqrt(x * x + y * y);
+    if (g.inner_edge < rc) {
+      out[0] = sol_pl(g.rho_c, g.rho_i, rc);
+    } else {
+      const double r2c = rc * rc;
+      out[0] = (g.rho_c * pow(g.inner_edge, g.rho_i - 4.0)) * (r2c * r2c);
+    }
+  } else {
+    double vgx = 0.0, vgy = 0.0;
+    const double mu = SOL_GAUSS2 * m0;
+    const double rc = sqrt(x * x + y * y);
+    const double vc = sqrt(mu / rc);
+    if (x == 0.0 && y == 0.0) {
+    } else if (y == 0.0) {
+      vgy = x > 0.0 ? vc : -vc;
+    } else if (x == 0.0) {
+      vgx = y > 0.0 ? -vc : vc;
+    } else if (x >= y) {
+      const double p = y / x;
+      vgy = x >= 0 ? vc / sqrt(1.0 + p * p) : -vc / sqrt(1.0 + p * p);
+      vgx = -vgy * p;
+    } else {
+      const double p = x / y;
+      vgx = y >= 0 ? -vc / sqrt(1.0 + p * p) : vc / sqrt(1.0 + p * p);
+      vgy = -vgx * p;
+    }
+    const double v = sqrt(1.0 - 2.0 * sol_pl(g.eta_c, g.eta_i, rc));
+    vgx *= v;
+    vgy *= v;
+    out[0] = vgx;
+    out[1] = vgy;
+  }
 }
 
 // One force evaluation of the CTA's sinks on the stage input V.yt (phases 1
@@ -188,12 +289,18 @@ __device__ __noinline__ void evaluate(const GroupArgs& P, const View& V, double 
   const ForceCtx& fc = P.fc;
   const int ns = P.ns, nsink = V.nsink;
   const bool home = blockIdx.x == 0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // phase 1: the three kinds of work in separate virtual warps
   const int w_rm3 = (nsink + 31) >> 5;
   const int w_pair = (V.npair + 31) >> 5;
-  const int w_gas = fc.gas.present ? (nsink + 31) >> 5 : 0;
-  for (int vw = warp; vw < w_rm3 + w_pair + w_gas; vw += nwarps) {
+  const int sidx = (flags & (SOL_EVAL_TYPE_I | SOL_EVAL_TYPE_II)) ? 0 : 1;
+  const bool drag = V.ndrag > 0 && (flags & SOL_EVAL_GAS_DRAG);
+  const int w_role = (V.ndrag + 31) >> 5;  // virtual warps per drag role
+  const int w_drag = V.ndrag > 0 ? 4 * w_role : 0;
+  const int nmine = warp < 4 ? V.sched_n[sidx * 4 + warp] : 0;
+  for (int t = 0; t < nmine; ++t) {
+    const int vw = V.sched[(sidx * 4 + warp) * kMaxVw + t];
+    if (!drag && vw >= w_rm3 + w_pair && vw < w_rm3 + w_pair + w_drag) continue;
     if (vw < w_rm3) {
       const int s = vw * 32 + lane;
       if (s < nsink) {
@@ -231,22 +338,48 @@ __device__ __noinline__ void evaluate(const GroupArgs& P, const View& V, double 
         V.pp[(1 * nsink + s) * ns + j] = yij * rijm3;
         V.pp[(2 * nsink + s) * ns + j] = zij * rijm3;
       }
-    } else {
-      const int s = (vw - w_rm3 - w_pair) * 32 + lane;
-      if (s < nsink && V.kind[s]) {
-        const int i = V.body[s], kind = V.kind[s];
-        gas_compute(fc, i, kind, V.yt + 6 * s, t, flags, V.gbuf + 3 * s, V.mig + s);
+    } else if (vw < w_rm3 + w_pair + w_drag) {  // drag: one role for 32 planetesimals
+      const int role = (vw - w_rm3 - w_pair) / w_role;
+      const int d = ((vw - w_rm3 - w_pair) - role * w_role) * 32 + lane;
+      if (d < V.ndrag) {
+        const int sd = V.dlist[d];
+        double o[2];
+        drag_role(fc.gas, role, fc.mass[0], V.yt + 6 * sd, o);
+        const int k0 = role == 0 ? 0 : role == 1 ? 2 : role == 2 ? 3 : 4;
+        V.dv[k0 * nsink + d] = o[0];
+        if (role == 0 || role == 3) V.dv[(k0 + 1) * nsink + d] = o[1];
+      }
+    } else {  // migration: a lane per massive body
+      const int m = (vw - w_rm3 - w_pair - w_drag) * 32 + lane;
+      if (m < V.nmig) {
+        const int s = V.mlist[m], i = V.body[s], kind = V.kind[s];
+        mig_compute(fc, i, kind, V.yt + 6 * s, V.factor, flags, V.gbuf + 3 * s, V.mig + s);
         if (s >= ns || home) {
           double* gb = global_gas_buf(fc, i, kind);
           gb[0] = V.gbuf[3 * s + 0];
           gb[1] = V.gbuf[3 * s + 1];
           gb[2] = V.gbuf[3 * s + 2];
-          if (kind >= 2) fc.mig_type[i] = V.mig[s];
+          fc.mig_type[i] = V.mig[s];
         }
       }
     }
   }
   __syncthreads();
+  if (drag) {  // phase 1b: the drag's regime part from the four roles, a lane per planetesimal
+    for (int d = threadIdx.x; d < V.ndrag; d += blockDim.x) {
+      const int sd = V.dlist[d], i = V.body[sd];
+      double out[3];
+      drag_finish(fc.gas, V.factor, V.m0pt, V.yt + 6 * sd, fc.radius[i], fc.density[i], fc.cd[i],
+                  fc.gamma_stokes[i], fc.gamma_epstein[i], V.dv[0 * nsink + d], V.dv[1 * nsink + d],
+                  V.dv[2 * nsink + d], V.dv[3 * nsink + d], V.dv[4 * nsink + d], V.dv[5 * nsink + d], out);
+      for (int k = 0; k < 3; ++k) V.gbuf[3 * sd + k] = out[k];
+      if (sd >= ns || home) {
+        double* gb = global_gas_buf(fc, i, 1);
+        for (int k = 0; k < 3; ++k) gb[k] = out[k];
+      }
+    }
+    __syncthreads();
+  }
   // phase 2: per (sink, component) the GravityAC sum, then the gas term
   double* fr = V.f + (size_t)r * 6 * nsink;
   for (int q = threadIdx.x; q < 3 * nsink; q += blockDim.x) {
@@ -335,6 +468,8 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
   V.nsrc = V.body + smax;
   V.kind = V.nsrc + smax;
   V.pair = V.kind + smax;
+  V.dlist = V.pair + smax * ns;
+  V.mlist = V.dlist + smax;
   const int nsink = V.nsink, ne = 6 * nsink;
   const bool home = blockIdx.x == 0;
   for (int s = threadIdx.x; s < nsink; s += blockDim.x) {
@@ -348,6 +483,11 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
     for (int k = 0; k < 3; ++k) V.gbuf[3 * s + k] = kind ? global_gas_buf(fc, i, kind)[k] : 0.0;
     if (s < ns) V.gm[s] = s >= 1 ? SOL_GAUSS2 * fc.mass[s] : 0.0;
   }
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    const int s = e / 6, k = e - 6 * s;
+    const int i = s < ns ? s : l0 + s - ns;
+    V.y0[e] = P.y0[6 * i + k];
+  }
   __syncthreads();
   if (threadIdx.x == 0) {  // the (sink, source) pairs of GravityAC: sinks i >= 1, sources 1 <= j < nsrc, j != i
     int np = 0;
@@ -359,13 +499,50 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
     }
     V.npair = np;
     S.npair = np;
-  }
-  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-    const int s = e / 6, k = e - 6 * s;
-    const int i = s < ns ? s : l0 + s - ns;
-    V.y0[e] = P.y0[6 * i + k];
-  }
-  if (threadIdx.x == 0) {
+    int nd = 0, nmg = 0;
+    for (int q = 0; q < nsink; ++q) {
+      if (V.kind[q] == 1) V.dlist[nd++] = q;
+      else if (V.kind[q] >= 2) V.mlist[nmg++] = q;
+    }
+    S.ndrag = nd;
+    S.nmig = nmg;
+    S.m0pt = fc.gas.present ? pow(fc.mass[0], fc.gas.pt) : 0.0;
+    // phase-1 schedules: the virtual warps (rm3, pairs, drag roles,
+    // migration) onto the four warps, longest first onto the least loaded
+    const int w_rm3 = (nsink + 31) >> 5, w_pair = (np + 31) >> 5;
+    const int w_role = (nd + 31) >> 5, w_drag = nd > 0 ? 4 * w_role : 0;
+    for (int sidx = 0; sidx < 2; ++sidx) {
+      const int w_mig = (sidx == 0 && nmg > 0) ? (nmg + 31) >> 5 : 0;
+      const int nvw = w_rm3 + w_pair + w_drag + w_mig;
+      int load[4] = {0, 0, 0, 0}, cnt[4] = {0, 0, 0, 0};
+      bool done[kMaxVw];
+      for (int vw = 0; vw < nvw; ++vw) done[vw] = false;
+      for (int it = 0; it < nvw; ++it) {
+        int pick = -1, pc = -1;
+        for (int vw = 0; vw < nvw; ++vw) {
+          if (done[vw]) continue;
+          int c2;
+          if (vw < w_rm3) c2 = kCostRm3;
+          else if (vw < w_rm3 + w_pair) c2 = kCostPair;
+          else if (vw < w_rm3 + w_pair + w_drag) {
+            const int role = (vw - w_rm3 - w_pair) / w_role;
+            c2 = role == 0 ? kCostRole0 : role == 1 ? kCostRole1 : role == 2 ? kCostRole2 : kCostRole3;
+          }
+          else c2 = kCostMig;
+          if (c2 > pc) {
+            pc = c2;
+            pick = vw;
+          }
+        }
+        done[pick] = true;
+        int wmin = 0;
+        for (int w = 1; w < 4; ++w)
+          if (load[w] < load[wmin]) wmin = w;
+        load[wmin] += pc;
+        S.sched[(sidx * 4 + wmin) * kMaxVw + cnt[wmin]++] = (unsigned char)pick;
+      }
+      for (int w = 0; w < 4; ++w) S.sched_n[sidx * 4 + w] = (unsigned char)cnt[w];
+    }
     const sol_ctrl c = *P.ctrl;
     S.t = c.t;
     S.h = c.h;
@@ -380,14 +557,23 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
   }
   __syncthreads();
   V.npair = S.npair;
+  V.ndrag = S.ndrag;
+  V.nmig = S.nmig;
+  V.m0pt = S.m0pt;
+  V.sched = S.sched;
+  V.sched_n = S.sched_n;
+  V.dv = smem + P.o_dv;
   bool ok = true;
   int parity = 0;  // partials are double-buffered: a slot is rewritten two barriers after it was read
   for (int step = 0; step < P.n_steps && ok && S.status == 0; ++step) {
     if (threadIdx.x == 0) {  // Driver: bodyData->h = timeLine->hNext (:74-75)
       S.h = S.h_next;
       S.accepted = 0;
+      // every stage of the step is evaluated at the step's start time
+      S.factor = fc.gas.present ? sol_reduction_factor(fc.gas, S.t) : 1.0;
     }
     __syncthreads();
+    V.factor = S.factor;
     // first evaluation with every term on (:77-82) and yscale (:87-89)
     for (int e = threadIdx.x; e < ne; e += blockDim.x) V.yt[e] = V.y0[e];
     __syncthreads();
@@ -535,8 +721,10 @@ size_t layout(GroupArgs& P, int nsink, int ns) {
   take(P.o_gbuf, (size_t)3 * nsink);
   take(P.o_red, (size_t)kBlock);
   take(P.o_mu, (size_t)nsink);
-  // ints: migType, body index, sources, gas kind (nsink each) and the pair list (nsink * ns)
-  take(P.o_int, ((size_t)4 * nsink + (size_t)nsink * ns + 1) / 2);
+  take(P.o_dv, (size_t)6 * nsink);
+  // ints: migType, body index, sources, gas kind (nsink each), the pair list (nsink * ns),
+  // the drag and migration lists (nsink each)
+  take(P.o_int, ((size_t)6 * nsink + (size_t)nsink * ns + 1) / 2);
   return o * sizeof(double);
 }
 
