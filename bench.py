@@ -238,9 +238,10 @@ def adjoint_section(local):
 def small_systems_section(local):
     """The latency-bound configurations: 256 bodies (1 star, 2 giants, 253 test
     particles; adaptive RKF78 eps 1e-10) and 8,193 bodies with a gas nebula
-    (1 star, 2 giants, 8,190 planetesimals with drag; eps 1e-11), FP64, each
-    driver call one CUDA graph with the attempt loop on the device; the
-    oracle on one core beside each."""
+    (1 star, 2 giants, 8,190 planetesimals with drag; eps 1e-11), FP64, every
+    driver call of the sequence in one cooperative launch of the group driver
+    (k_group_rkf78: stage work spread over lanes and SM sub-partitions, the
+    few sources integrated by every CTA); the oracle on one core beside each."""
     import oracle
     from solaris_gb300 import abi, engine, scenarios
     out = {}

@@ -6,7 +6,7 @@ Cases (each sized to a few hundred MB of device memory at most):
   fp64_few       k_gravity_ac_few: FP64 force, 4,096 self-gravitating bodies
   split_ff_warp  k_pairs_few<SPLIT_FF>: float-float force, 4,096 bodies
   split_ff_2d    k_pairs<SPLIT_FF> + k_combine: float-float force, 32,768 bodies
-  persistent     k_persist_rkf78: 20 RKF78 driver calls of 1 star + 2 giants +
+  persistent     k_group_rkf78: 20 RKF78 driver calls of 1 star + 2 giants +
                  253 test particles in one cooperative launch
   ensemble       k_ensemble_rkf78: 2 driver calls of 512 small systems
   adjoint        k_vjp: forward and backward of 20 fixed RKF78 steps,
