@@ -20,9 +20,10 @@
 // whatever the number of active lanes, and a stage is a dependent chain of
 // ~175 FP64 instructions per body (IEEE sqrt and division of rm3 and of each
 // pair, the stage sums), ~7-9 us whatever the bodies per CTA (measured from 1
-// to 128).  One 256-body system therefore runs ~150 us per RKF78 attempt
-// here, 1.7x the graph path; batches of such systems belong to the ensemble
-// kernel.
+// to 128).  The group driver (sol_group.cu) spreads that chain over lanes and
+// SM sub-partitions and takes every system it can hold (about 3x faster);
+// this one-thread-per-body form remains for systems with more light bodies
+// than the group layout holds.
 //
 // Grid barriers spin on a generation counter with an iteration limit; a CTA
 // that runs out raises SOL_DEV_TIMEOUT and an abort flag that makes every
