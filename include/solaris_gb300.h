@@ -363,6 +363,41 @@ int sol_get_bodies(sol_ctx* ctx, sol_nbodies* counts, int32_t* id, int32_t* type
  * 6 + 6 doubles of phases, double time) to path. */
 int sol_write_affairs(const char* path, const sol_affair* affairs, int32_t n, int32_t first_event_id);
 
+/* ---- the Simulator's step loop between host work ---------------------------
+ * Simulator::Integrate / DecisionMaking (Solaris/Simulator.cpp:121-250) for
+ * the steps at which the host has nothing to do.  After each accepted driver
+ * step: steps += 1, elapsed and last_save += h_did; then
+ *   SOL_STOP_EVENT  when an event predicate of CheckEvent holds on the step's
+ *                   last evaluation (rm3 < 1 / R_ej^3, rm3 > 1 / R_hc^3,
+ *                   factor (R_i + R_NN) > d_NN; a parameter <= 0 is off):
+ *                   the rest of DecisionMaking is the host's;
+ *   SOL_STOP_LENGTH when |clock| >= |length| (clock: time, or elapsed when
+ *                   relative_end != 0);
+ * otherwise h_next is clamped to the end of the phase, then
+ *   SOL_STOP_OUTPUT when |last_save| >= |output| (a record is due; the host
+ *                   saves, sets last_save = 0 and clamps h_next to the next
+ *                   output);
+ * otherwise h_next is clamped to the next output and, every 100 steps of the
+ * run (steps % 100 == 0), state components below 1e-50 are set to zero
+ * (Tools::CheckAgainstSmallestNumber); after max_steps such steps
+ * SOL_STOP_STEPS.  The stopping step's smallest-number flush is the host's. */
+typedef struct sol_sim_line {
+  double time, length, output;
+  double h_next, h_did;
+  double elapsed, last_save;
+  int64_t steps;
+  int32_t relative_end, pad;
+} sol_sim_line;
+enum { SOL_STOP_STEPS = 0, SOL_STOP_EVENT = 1, SOL_STOP_LENGTH = 2, SOL_STOP_OUTPUT = 3 };
+int sol_run_until(sol_ctx* ctx, int32_t integrator, sol_sim_line* line, int32_t max_steps, double ejection,
+                  double hit_centrum, double collision_factor, int32_t* reason, sol_step_stats* stats);
+/* Tools::CheckAgainstSmallestNumber on the resident state: |y| < 1e-50 -> 0. */
+int sol_flush_smallest(sol_ctx* ctx);
+/* After sol_run_until with collision_factor > 0: the state at the start of
+ * the last step (bodyData.y after the swap, which the reference's collision
+ * records carry), 6N doubles. */
+int sol_get_step_start(sol_ctx* ctx, double* y);
+
 /* ---- initial conditions in bulk ------------------------------------------
  * Ephemeris::CalculatePhase with Ephemeris::KeplerEquationSolver
  * (Solaris/Ephemeris.cpp:141-211) for n bodies on the device, one thread per

@@ -88,6 +88,15 @@ class SolTimeLine(C.Structure):
     _fields_ = [("time", C.c_double), ("h_next", C.c_double), ("h_did", C.c_double)]
 
 
+class SolSimLine(C.Structure):
+    _fields_ = [("time", C.c_double), ("length", C.c_double), ("output", C.c_double), ("h_next", C.c_double),
+                ("h_did", C.c_double), ("elapsed", C.c_double), ("last_save", C.c_double), ("steps", C.c_int64),
+                ("relative_end", C.c_int32), ("pad", C.c_int32)]
+
+
+STOP_STEPS, STOP_EVENT, STOP_LENGTH, STOP_OUTPUT = 0, 1, 2, 3
+
+
 class SolStepStats(C.Structure):
     _fields_ = [("accepted", C.c_int64), ("rejected", C.c_int64), ("evaluations", C.c_int64)]
 
@@ -222,6 +231,10 @@ def _declare(lib):
                                         C.c_int32, C.POINTER(C.c_int32)]),
         "sol_get_bodies": (C.c_int, [P, C.POINTER(SolNBodies), _PI32, _PI32, _PF64, _PF64, _PF64]),
         "sol_write_affairs": (C.c_int, [C.c_char_p, C.POINTER(SolAffair), C.c_int32, C.c_int32]),
+        "sol_run_until": (C.c_int, [P, C.c_int32, C.POINTER(SolSimLine), C.c_int32, C.c_double, C.c_double,
+                                    C.c_double, C.POINTER(C.c_int32), C.POINTER(SolStepStats)]),
+        "sol_flush_smallest": (C.c_int, [P]),
+        "sol_get_step_start": (C.c_int, [P, _PF64]),
         "sol_gravity_noalloc": (C.c_int, [C.POINTER(SolNBodies), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     }
@@ -247,7 +260,7 @@ def exported_names():
         "sol_get_driver_vectors", "sol_get_side_buffers", "sol_bench_stages", "sol_output_open",
         "sol_output_save_phases", "sol_output_save_integrals", "sol_output_flush", "sol_output_close",
         "sol_format_phases_record", "sol_format_integrals_record", "sol_phases_from_elements",
-        "sol_handle_events", "sol_get_bodies", "sol_write_affairs"]
+        "sol_handle_events", "sol_get_bodies", "sol_write_affairs", "sol_run_until", "sol_flush_smallest", "sol_get_step_start"]
 
 
 def load_library(path: str | None = None):

@@ -146,6 +146,8 @@ void free_ctx(sol_ctx* c) {
   for (int k = 0; k < 2; ++k) sol_graph_release(c->graphs[k]);
   sol_adjoint_free(c->adj);
   if (c->d_persist) cudaFree(c->d_persist);
+  if (c->d_sim) cudaFree(c->d_sim);
+  if (c->d_ystart) cudaFree(c->d_ystart);
   free(c->h_id);
   if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -571,6 +573,183 @@ int sol_get_last_eval(sol_ctx* c, double* rm3, int32_t* nn_idx, double* nn_dist)
   if (rm3) SOL_CUDA(cudaMemcpy(rm3, c->d_rm3, sizeof(double) * c->n, cudaMemcpyDeviceToHost));
   if (nn_idx) SOL_CUDA(cudaMemcpy(nn_idx, c->d_nn_idx, sizeof(int32_t) * c->n, cudaMemcpyDeviceToHost));
   if (nn_dist) SOL_CUDA(cudaMemcpy(nn_dist, c->d_nn_dist, sizeof(double) * c->n, cudaMemcpyDeviceToHost));
+  return SOL_OK;
+}
+
+namespace {
+
+constexpr double kSmallestNumber = 1.0e-50;  // Solaris/Constants.h:17
+constexpr long long kCheckForSm = 100;       // Solaris/Constants.h:16
+
+__global__ void k_flush_smallest(int nv, double* __restrict__ y) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nv; e += gridDim.x * blockDim.x)
+    if (fabs(y[e]) < kSmallestNumber) y[e] = 0.0;
+}
+
+int flush_launch(sol_ctx* c) {
+  const int g = std::min((c->nv + 255) / 256, 1024);
+  k_flush_smallest<<<g, 256, 0, c->stream>>>(c->nv, c->d_y0);
+  SOL_LAUNCHED();
+  return SOL_OK;
+}
+
+// Whether an event predicate of CheckEvent holds on the last evaluation.
+int events_pending(sol_ctx* c, double ej, double hc, double cf, bool* pending) {
+  *pending = false;
+  if (!(ej > 0.0) && !(hc > 0.0) && !(cf > 0.0)) return SOL_OK;
+  int* d_cnt = static_cast<int*>(c->d_sim);
+  RET(sol_events_launch(c, c->d_y0, ej, hc, cf, nullptr, 0, d_cnt));
+  int cnt = 0;
+  SOL_CUDA(cudaMemcpyAsync(&cnt, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  SOL_CUDA(cudaStreamSynchronize(c->stream));
+  *pending = cnt > 0;
+  return SOL_OK;
+}
+
+// sol_sim_line + stop reason + event flags of the group driver
+constexpr size_t kSimBytes = 256 + sizeof(int) * 2 * kGroupMaxCtas;
+
+int ensure_sim(sol_ctx* c) {
+  if (!c->d_sim) {
+    if (cudaMalloc(&c->d_sim, kSimBytes) != cudaSuccess) {
+      sol_set_error("cudaMalloc of the step-loop scratch failed");
+      return SOL_ERR_NOMEM;
+    }
+    SOL_CUDA(cudaMemset(c->d_sim, 0, kSimBytes));
+  }
+  if (!c->d_ystart) {  // bodies are only ever removed: the first size holds
+    if (cudaMalloc((void**)&c->d_ystart, sizeof(double) * (size_t)c->nv) != cudaSuccess) {
+      sol_set_error("cudaMalloc of the step-start state failed");
+      return SOL_ERR_NOMEM;
+    }
+  }
+  return SOL_OK;
+}
+
+}  // namespace
+
+int sol_get_step_start(sol_ctx* c, double* y) {
+  RET(check_ctx(c));
+  if (!y || !c->d_ystart) {
+    sol_set_error("sol_get_step_start: no step loop with collisions has run");
+    return SOL_ERR_STATE;
+  }
+  RET(set_device(c));
+  SOL_CUDA(cudaMemcpyAsync(y, c->d_ystart, sizeof(double) * (size_t)c->nv, cudaMemcpyDeviceToHost, c->stream));
+  SOL_CUDA(cudaStreamSynchronize(c->stream));
+  return SOL_OK;
+}
+
+int sol_flush_smallest(sol_ctx* c) {
+  RET(check_ctx(c));
+  if (!c->state_valid) {
+    sol_set_error("no state: call sol_set_state first");
+    return SOL_ERR_STATE;
+  }
+  RET(set_device(c));
+  RET(flush_launch(c));
+  SOL_CUDA(cudaStreamSynchronize(c->stream));
+  return SOL_OK;
+}
+
+int sol_run_until(sol_ctx* c, int32_t integrator, sol_sim_line* L, int32_t max_steps, double ejection,
+                  double hit_centrum, double collision_factor, int32_t* reason, sol_step_stats* stats) {
+  RET(check_ctx(c));
+  if (!L || !reason || max_steps < 1) {
+    sol_set_error("sol_run_until: bad arguments");
+    return SOL_ERR_ARG;
+  }
+  if (!c->state_valid) {
+    sol_set_error("no state: call sol_set_state first");
+    return SOL_ERR_STATE;
+  }
+  RET(set_device(c));
+  RET(ensure_sim(c));
+  const double e3 = ejection > 0 ? 1.0 / (ejection * ejection * ejection) : 0.0;
+  const double h3 = hit_centrum > 0 ? 1.0 / (hit_centrum * hit_centrum * hit_centrum) : 0.0;
+  // the whole loop on the device: RKF78 systems of few sources
+  if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78 && c->device_loop && sol_group_eligible(c)) {
+    char* base = static_cast<char*>(c->d_sim);
+    GroupSim sim;
+    sim.e3 = e3;
+    sim.h3 = h3;
+    sim.cf = collision_factor > 0 ? collision_factor : 0.0;
+    sim.line = reinterpret_cast<sol_sim_line*>(base);
+    sim.reason = reinterpret_cast<int*>(base + 128);
+    sim.ev = reinterpret_cast<int*>(base + 256);
+    sim.yprev = collision_factor > 0 ? c->d_ystart : nullptr;
+    sol_ctrl h0;
+    memset(&h0, 0, sizeof(h0));
+    h0.t = L->time;
+    h0.h_next = L->h_next;
+    h0.h_did = L->h_did;
+    h0.h = L->h_next;
+    h0.eps = c->eps;
+    const int stop_steps = SOL_STOP_STEPS;
+    SOL_CUDA(cudaMemcpyAsync(c->d_ctrl, &h0, sizeof(h0), cudaMemcpyHostToDevice, c->stream));
+    SOL_CUDA(cudaMemcpyAsync(sim.line, L, sizeof(*L), cudaMemcpyHostToDevice, c->stream));
+    SOL_CUDA(cudaMemcpyAsync(sim.reason, &stop_steps, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    const int r = sol_group_rkf78(c, max_steps, &sim);
+    if (r != SOL_ERR_STATE) {
+      if (r != SOL_OK) return r;
+      SOL_CUDA(cudaMemcpyAsync(c->h_ctrl, c->d_ctrl, sizeof(sol_ctrl), cudaMemcpyDeviceToHost, c->stream));
+      SOL_CUDA(cudaMemcpyAsync(L, sim.line, sizeof(*L), cudaMemcpyDeviceToHost, c->stream));
+      SOL_CUDA(cudaMemcpyAsync(reason, sim.reason, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      SOL_CUDA(cudaStreamSynchronize(c->stream));
+      const sol_ctrl& hc = *c->h_ctrl;
+      c->last_eval_valid = 1;
+      if (stats) {
+        stats->accepted += hc.n_accepted;
+        stats->rejected += hc.n_rejected;
+        stats->evaluations += hc.n_accepted * 13 + hc.n_rejected * 12;
+      }
+      if (hc.dev_status & SOL_DEV_TIMEOUT) {
+        sol_set_error("a bounded device wait ran out");
+        return SOL_ERR_TIMEOUT;
+      }
+      if (hc.dev_status & SOL_DEV_UNDERFLOW) {
+        sol_set_error("Stepsize-underflow occurred during Runge-Kutta-Fehlberg7(8) step!");
+        return SOL_ERR_UNDERFLOW;
+      }
+      return SOL_OK;
+    }
+  }
+  // any other integrator or path: the same loop on the host, one driver call per step
+  for (int k = 0; k < max_steps; ++k) {
+    if (collision_factor > 0)
+      SOL_CUDA(cudaMemcpyAsync(c->d_ystart, c->d_y0, sizeof(double) * (size_t)c->nv, cudaMemcpyDeviceToDevice,
+                               c->stream));
+    sol_time_line tl = {L->time, L->h_next, L->h_did};
+    RET(sol_driver(c, integrator, &tl, 1, stats));
+    L->time = tl.time;
+    L->h_next = tl.h_next;
+    L->h_did = tl.h_did;
+    L->steps += 1;
+    L->elapsed += L->h_did;
+    L->last_save += L->h_did;
+    bool pending = false;
+    RET(events_pending(c, ejection, hit_centrum, collision_factor, &pending));
+    if (pending) {
+      *reason = SOL_STOP_EVENT;
+      return SOL_OK;
+    }
+    const double clock = L->relative_end ? L->elapsed : L->time;
+    if (fabs(clock) >= fabs(L->length)) {
+      *reason = SOL_STOP_LENGTH;
+      return SOL_OK;
+    }
+    if (fabs(clock + L->h_next) > fabs(L->length)) L->h_next = L->length - clock;
+    if (fabs(L->last_save) >= fabs(L->output)) {
+      *reason = SOL_STOP_OUTPUT;
+      return SOL_OK;
+    }
+    if (fabs(L->last_save + L->h_next) > fabs(L->output)) L->h_next = L->output - L->last_save;
+    if (L->steps % kCheckForSm == 0) {
+      RET(flush_launch(c));
+    }
+  }
+  SOL_CUDA(cudaStreamSynchronize(c->stream));
+  *reason = SOL_STOP_STEPS;
   return SOL_OK;
 }
 

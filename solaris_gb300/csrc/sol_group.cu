@@ -75,6 +75,12 @@ struct GroupArgs {
   int ns;               // sources: nm + n_spl
   int local;            // other bodies per CTA
   int n_steps;
+  int sim;              // the Simulator's step loop (sol_run_until)
+  double e3, h3, cf;    // its event thresholds (0: off)
+  sol_sim_line* line;
+  int* reason;
+  int* ev;              // per-CTA event flags, double-buffered
+  double* yprev;        // the state at the start of a step that stops with an event (or null)
   // shared-memory layout (offsets in doubles)
   int o_f, o_y0, o_yt, o_ys, o_yn, o_rm3, o_pp, o_prb, o_xr, o_gm, o_gbuf, o_red, o_mu, o_dv, o_int;
 };
@@ -116,6 +122,8 @@ struct Ctl {
   long long n_acc, n_rej;
   int status, accepted, abort, npair, ndrag, nmig;
   double m0pt, factor;
+  int event, stop, reason, flush;
+  sol_sim_line L;
   unsigned char sched_n[8];
   unsigned char sched[8 * kMaxVw];
 };
@@ -147,6 +155,7 @@ struct View {
   double factor, m0pt;  // ReductionFactor at the step's time, m0^pt
   const unsigned char* sched;  // [2][4][kMaxVw]: virtual warps of each warp (0: with migration, 1: without)
   const unsigned char* sched_n;  // [2][4]
+  int* event;                    // set when an event predicate holds on the attempt's last evaluation
   double* dv;                    // [6][nsink]: the drag's partial results of each planetesimal
 };
 
@@ -423,6 +432,12 @@ __device__ __noinline__ void evaluate(const GroupArgs& P, const View& V, double 
       }
       fc.nn_idx[i] = nn;
       fc.nn_dist[i] = nn >= 0 ? __longlong_as_double(rminb) : 0.0;
+      if (P.sim && r == 12) {  // CheckEvent's predicates on the attempt's last evaluation
+        const double rm3 = V.rm3[s];
+        const bool ev = (P.e3 > 0.0 && rm3 < P.e3) || (P.h3 > 0.0 && rm3 > P.h3) ||
+                        (P.cf > 0.0 && nn >= 0 && P.cf * (fc.radius[i] + fc.radius[nn]) > __longlong_as_double(rminb));
+        if (ev) atomicOr(V.event, 1);
+      }
     }
   }
   __syncthreads();
@@ -554,6 +569,11 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
     S.n_rej = c.n_rejected;
     S.status = c.dev_status;
     S.abort = 0;
+    S.event = 0;
+    S.stop = 0;
+    S.reason = SOL_STOP_STEPS;
+    S.flush = 0;
+    if (P.sim) S.L = *P.line;
   }
   __syncthreads();
   V.npair = S.npair;
@@ -562,10 +582,11 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
   V.m0pt = S.m0pt;
   V.sched = S.sched;
   V.sched_n = S.sched_n;
+  V.event = &S.event;
   V.dv = smem + P.o_dv;
   bool ok = true;
   int parity = 0;  // partials are double-buffered: a slot is rewritten two barriers after it was read
-  for (int step = 0; step < P.n_steps && ok && S.status == 0; ++step) {
+  for (int step = 0; step < P.n_steps && ok && S.status == 0 && !S.stop; ++step) {
     if (threadIdx.x == 0) {  // Driver: bodyData->h = timeLine->hNext (:74-75)
       S.h = S.h_next;
       S.accepted = 0;
@@ -624,8 +645,12 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
         __syncthreads();
       }
       double* partial = P.partial + (size_t)parity * gridDim.x;
+      int* evp = P.sim ? P.ev + (size_t)parity * gridDim.x : nullptr;
       parity ^= 1;
-      if (threadIdx.x == 0) partial[blockIdx.x] = V.red[0];
+      if (threadIdx.x == 0) {
+        partial[blockIdx.x] = V.red[0];
+        if (P.sim) evp[blockIdx.x] = S.event;
+      }
       ok = group_barrier(P, &S.abort);
       if (!ok) break;
       if (threadIdx.x == 0) {  // every CTA takes the same decision (:98-133)
@@ -643,6 +668,35 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
           S.h = S.h_next;
           S.accepted = 1;
           S.n_acc++;
+          if (P.sim) {  // Simulator::DecisionMaking up to where the host has work (Simulator.cpp:181-250)
+            int any = 0;
+            for (int b = 0; b < (int)gridDim.x; ++b) any |= gridDim.x > 1 ? __ldcg(evp + b) : S.event;
+            sol_sim_line& L = S.L;
+            L.steps += 1;
+            L.elapsed += S.h_did;
+            L.last_save += S.h_did;
+            S.flush = 0;
+            if (any) {
+              S.reason = SOL_STOP_EVENT;
+              S.stop = 1;
+            } else {
+              const double clock = L.relative_end ? L.elapsed : S.t;
+              if (fabs(clock) >= fabs(L.length)) {
+                S.reason = SOL_STOP_LENGTH;
+                S.stop = 1;
+              } else {
+                if (fabs(clock + S.h_next) > fabs(L.length)) S.h_next = L.length - clock;
+                if (fabs(L.last_save) >= fabs(L.output)) {
+                  S.reason = SOL_STOP_OUTPUT;
+                  S.stop = 1;
+                } else {
+                  if (fabs(L.last_save + S.h_next) > fabs(L.output)) S.h_next = L.output - L.last_save;
+                  S.flush = (L.steps % 100) == 0;  // Tools::CheckAgainstSmallestNumber every CheckForSM steps
+                }
+              }
+            }
+            S.h = S.h_next;
+          }
         } else {
           S.n_rej++;
           const double hTemp = 0.9 * h * pow(em, -0.25);
@@ -650,13 +704,18 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
           S.h = hn;
           if (S.t + hn == S.t) S.status |= SOL_DEV_UNDERFLOW;
         }
+        S.event = 0;
       }
       __syncthreads();
       if (S.accepted) {
+        const bool keep_start = P.sim && P.yprev && S.stop && S.reason == SOL_STOP_EVENT;
         for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-          V.y0[e] = V.yn[e];
+          double v = V.yn[e];
           const int s = e / 6;
-          if (s >= ns || home) P.y0[6 * V.body[s] + (e - 6 * s)] = V.yn[e];
+          if (keep_start && (s >= ns || home)) P.yprev[6 * V.body[s] + (e - 6 * s)] = V.y0[e];
+          if (S.flush && fabs(v) < 1.0e-50) v = 0.0;
+          V.y0[e] = v;
+          if (s >= ns || home) P.y0[6 * V.body[s] + (e - 6 * s)] = v;
         }
         __syncthreads();
         break;
@@ -675,6 +734,14 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
     c->n_accepted = S.n_acc;
     c->n_rejected = S.n_rej;
     atomicOr(&c->dev_status, S.status);
+    if (P.sim) {
+      sol_sim_line L = S.L;
+      L.time = S.t;
+      L.h_next = S.h_next;
+      L.h_did = S.h_did;
+      *P.line = L;
+      *P.reason = S.stop ? S.reason : SOL_STOP_STEPS;
+    }
   }
 }
 
@@ -739,7 +806,7 @@ int sol_group_eligible(const sol_ctx* c) {
 
 // n_steps RKF78 driver calls in one cooperative launch of the group kernel.
 // Returns SOL_ERR_STATE (nothing launched) when the system does not fit.
-int sol_group_rkf78(sol_ctx* c, int n_steps) {
+int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim) {
   if (!sol_group_eligible(c)) return SOL_ERR_STATE;
   if (!c->d_persist) {
     const size_t doubles = 2 * 7 * 32 + 4096 + 8;
@@ -793,6 +860,17 @@ int sol_group_rkf78(sol_ctx* c, int n_steps) {
   P.ns = ns;
   P.local = local;
   P.n_steps = n_steps;
+  if (sim) {
+    if (grid > kGroupMaxCtas) return SOL_ERR_STATE;
+    P.sim = 1;
+    P.e3 = sim->e3;
+    P.h3 = sim->h3;
+    P.cf = sim->cf;
+    P.line = sim->line;
+    P.reason = sim->reason;
+    P.ev = sim->ev;
+    P.yprev = sim->yprev;
+  }
   SOL_CUDA(cudaMemsetAsync(words, 0, 4 * sizeof(unsigned), c->stream));
   void* args[] = {&P};
   SOL_CUDA(cudaLaunchCooperativeKernel((const void*)k_group_rkf78, grid, kBlock, args, smem, c->stream));

@@ -168,6 +168,8 @@ struct sol_ctx {
   int graph_used;
   sol_adjoint_state* adj;  // checkpoints and buffers of the discrete adjoint
   double* d_persist;       // source tables, block maxima and barrier words of the persistent driver
+  void* d_sim;             // the step loop's line, stop reason and event flags (sol_run_until)
+  double* d_ystart;        // the state at the start of the last step of sol_run_until (collision records)
   int32_t* h_id;           // BodyData::id on the host (output records carry ids)
 };
 
@@ -192,7 +194,18 @@ const Rkf78Table& sol_rkf78_table();
 int sol_persist_eligible(const sol_ctx* c);
 int sol_persist_rkf78(sol_ctx* c, int n_steps);
 int sol_group_eligible(const sol_ctx* c);
-int sol_group_rkf78(sol_ctx* c, int n_steps);
+// The Simulator's step loop inside the group driver (sol_run_until): event
+// thresholds (0: off), and device memory for the line, the stop reason and
+// double-buffered per-CTA event flags.
+struct GroupSim {
+  double e3, h3, cf;
+  sol_sim_line* line;
+  int* reason;
+  int* ev;        // [2 * kGroupMaxCtas]
+  double* yprev;  // when not null: the state at the start of the step that stops with an event
+};
+constexpr int kGroupMaxCtas = 2048;
+int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim = nullptr);
 int sol_fp64_peak_launch(int device, double* flops);
 
 // ---- PTX helpers: bulk copies (TMA engine) with mbarrier completion --------

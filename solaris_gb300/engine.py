@@ -103,6 +103,25 @@ class Context:
         return dict(time=tl.time, h_next=tl.h_next, h_did=tl.h_did,
                     stats=(st.accepted, st.rejected, st.evaluations), time_line=tl)
 
+    def run_until(self, integrator, line, max_steps, ejection=0.0, hit_centrum=0.0, collision_factor=0.0):
+        """The Simulator's step loop until the host has work (sol_run_until):
+        updates line (abi.SolSimLine) and returns the stop reason and the
+        (accepted, rejected, evaluations) counters."""
+        reason = C.c_int32(0)
+        st = abi.SolStepStats()
+        abi.check(self.lib, self.lib.sol_run_until(self.h, int(integrator), C.byref(line), int(max_steps),
+                                                   float(ejection), float(hit_centrum), float(collision_factor),
+                                                   C.byref(reason), C.byref(st)))
+        return reason.value, (st.accepted, st.rejected, st.evaluations)
+
+    def flush_smallest(self):
+        abi.check(self.lib, self.lib.sol_flush_smallest(self.h))
+
+    def step_start(self):
+        y = np.empty(6 * self.n)
+        abi.check(self.lib, self.lib.sol_get_step_start(self.h, abi.f64p(y)))
+        return y
+
     def rkf78_step(self, t, h, y0):
         y0 = np.ascontiguousarray(y0, dtype=np.float64)
         y, err, em = np.empty(6 * self.n), np.empty(6 * self.n), np.zeros(1)

@@ -72,6 +72,27 @@ class EngineBackend:
     def events(self, time, ejection, hit_centrum, collision_factor):
         return self.ctx.handle_events(time, ejection, hit_centrum, collision_factor)
 
+    def run_until(self, sim, tl, clock, max_steps: int = 1 << 20) -> int:
+        """Steps on the device until the host has work (sol_run_until)."""
+        st = sim.sc.settings
+        rel = sim.relative_end_test
+        line = abi.SolSimLine(time=tl.time, length=tl.length, output=tl.output, h_next=tl.h_next, h_did=tl.h_did,
+                              elapsed=clock.all if rel else tl.elapsed,
+                              last_save=clock.save if rel else tl.last_save, steps=sim.steps,
+                              relative_end=1 if rel else 0)
+        factor = st.collision if st.collision is not None else 0.0
+        reason, _ = self.ctx.run_until(self.integrator, line, max_steps, st.ejection, st.hit_centrum, factor)
+        tl.time, tl.h_next, tl.h_did = line.time, line.h_next, line.h_did
+        if rel:
+            clock.all, clock.save = line.elapsed, line.last_save
+        else:
+            tl.elapsed, tl.last_save = line.elapsed, line.last_save
+        sim.steps = int(line.steps)
+        return reason
+
+    def step_start(self):
+        return self.ctx.step_start()
+
     def n_total(self) -> int:
         return self.ctx.n
 
@@ -133,6 +154,13 @@ class _Body:
         self.density = spec.density if spec.type != abi.TEST_PARTICLE else 0.0
         self.components = [Component(c.name, c.ratio) for c in spec.components]
         self.phase = list(spec.phase)
+
+
+@dataclasses.dataclass
+class _Clock:
+    """Time integrated in the current phase (all) and since its last record (save)."""
+    all: float = 0.0
+    save: float = 0.0
 
 
 @dataclasses.dataclass
@@ -340,38 +368,28 @@ class Simulator:
         self.be = be = self.factory(system, st, self.dir)
         self.phases += 1
         collisions = st.collision is not None
-        sum_all = sum_save = 0.0  # the phase-relative clock of relative_end_test
+        clock = _Clock()  # the phase-relative clock of relative_end_test
+        chunked = hasattr(be, "run_until")
         try:
             be.save_phases(tl.time)
             be.save_integrals(tl.time)
             while True:
-                y_start = be.state() if collisions else None
-                tl.time, tl.h_did, tl.h_next = be.step(tl.time, tl.h_next)
-                self.steps += 1
-                tl.elapsed += tl.h_did
-                tl.last_save += tl.h_did
-                sum_all += tl.h_did
-                sum_save += tl.h_did
-                self._check_event(tl.time, y_start)
-                clock = sum_all if self.relative_end_test else tl.time  # 1000 YearToDay millenium + time
-                since = sum_save if self.relative_end_test else tl.last_save
-                stop = False
-                if abs(clock) >= abs(tl.length):
-                    stop = True
-                elif be.n_total() <= 1:
-                    self._log("The total number of bodies reduced to 1!")
-                    stop = True
+                if chunked:  # the steps without host work run on the device
+                    reason = be.run_until(self, tl, clock)
+                    if reason == abi.STOP_STEPS:
+                        continue
+                    y_start = be.step_start() if collisions and reason == abi.STOP_EVENT else None
+                    events = reason == abi.STOP_EVENT
                 else:
-                    if abs(clock + tl.h_next) > abs(tl.length):
-                        tl.h_next = tl.length - clock
-                    if abs(since) >= abs(tl.output):
-                        be.save_phases(tl.time)
-                        be.save_integrals(tl.time)
-                        tl.last_save = sum_save = since = 0.0
-                        if self.relative_end_test:
-                            tl.save += tl.output
-                    if abs(since + tl.h_next) > abs(tl.output):
-                        tl.h_next = tl.output - since
+                    y_start = be.state() if collisions else None
+                    tl.time, tl.h_did, tl.h_next = be.step(tl.time, tl.h_next)
+                    self.steps += 1
+                    tl.elapsed += tl.h_did
+                    tl.last_save += tl.h_did
+                    clock.all += tl.h_did
+                    clock.save += tl.h_did
+                    events = True
+                stop = self._decision(tl, clock, y_start, events)
                 if self.steps % CHECK_FOR_SMALLEST == 0:
                     be.zero_below_smallest()
                 if stop:
@@ -385,6 +403,31 @@ class Simulator:
         finally:
             be.close()
             self.be = None
+
+    def _decision(self, tl: TimeLine, clock: "_Clock", y_start, events: bool) -> bool:
+        """Simulator::DecisionMaking (Simulator.cpp:181-250) after the step's
+        times are added: CheckEvent, the end test, the clamps and the record."""
+        be = self.be
+        if events:
+            self._check_event(tl.time, y_start)
+        now = clock.all if self.relative_end_test else tl.time  # 1000 YearToDay millenium + time
+        since = clock.save if self.relative_end_test else tl.last_save
+        if abs(now) >= abs(tl.length):
+            return True
+        if be.n_total() <= 1:
+            self._log("The total number of bodies reduced to 1!")
+            return True
+        if abs(now + tl.h_next) > abs(tl.length):
+            tl.h_next = tl.length - now
+        if abs(since) >= abs(tl.output):
+            be.save_phases(tl.time)
+            be.save_integrals(tl.time)
+            tl.last_save = clock.save = since = 0.0
+            if self.relative_end_test:
+                tl.save += tl.output
+        if abs(since + tl.h_next) > abs(tl.output):
+            tl.h_next = tl.output - since
+        return False
 
     # -- Simulator::Run ------------------------------------------------------------------------
     def _synchronization(self, main: TimeLine):

@@ -51,7 +51,7 @@ def test_scenario_on_the_device(tmp_path, name):
     out = str(tmp_path)
     k0 = engine.kernel_launches()
     r = sim.Simulator(sc, directory=out).run()
-    assert engine.kernel_launches() - k0 > r["steps"]  # the steps ran on the device
+    assert engine.kernel_launches() - k0 >= r["phases"]  # the steps ran on the device (many per launch)
     gold = golden_dir(name)
     assert sorted(f for f in os.listdir(out) if f != st.log) == sorted(os.listdir(gold))
 
