@@ -103,3 +103,34 @@ def test_scenario_on_the_device(tmp_path, name):
             r, v = np.linalg.norm(a[k][:3]), np.linalg.norm(a[k][3:])
             assert np.linalg.norm(a[k][:3] - b[k][:3]) <= 4.0 * v * dt + PHASE_RTOL * r, k
             assert np.linalg.norm(a[k][3:] - b[k][3:]) <= 1e-6 * v, k
+
+
+class _OneStepAtATime:
+    """The device context driven one host call per step (the reference loop's shape)."""
+
+    def __init__(self, system, st, directory):
+        self.b = sim.EngineBackend(system, st, directory)
+
+    def __getattr__(self, k):
+        if k in ("run_until", "step_start"):
+            raise AttributeError(k)
+        return getattr(self.b, k)
+
+
+@pytest.mark.parametrize("name", ["collision_rkf78", "epochs_rkf78", "gas_rk4"])
+def test_device_step_loop_matches_host_step_loop(tmp_path, name):
+    """sol_run_until (DecisionMaking's clamps, the event predicates and the
+    smallest-number flush on the device) writes the same bytes as the same
+    device driver called once per step from the host."""
+    outs = []
+    for k, backend in enumerate((None, _OneStepAtATime)):
+        sc = sx.load(xml_path(name))
+        d = tmp_path / f"run{k}"
+        kw = {} if backend is None else {"backend": backend}
+        r = sim.Simulator(sc, directory=str(d), **kw).run()
+        files = {f: (d / f).read_bytes() for f in sorted(os.listdir(d)) if f != sc.settings.log}
+        outs.append((r["steps"], len(r["affairs"]), files))
+    assert outs[0][0] == outs[1][0] and outs[0][1] == outs[1][1]
+    assert outs[0][2].keys() == outs[1][2].keys()
+    for f in outs[0][2]:
+        assert outs[0][2][f] == outs[1][2][f], f
