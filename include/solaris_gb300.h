@@ -469,6 +469,19 @@ int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_type, const 
 /* ---- measurement helpers ------------------------------------------------ */
 /* Measured FP64 fused-multiply-add throughput of this GPU in FLOP/s (FMA = 2). */
 int sol_measure_fp64_peak(int32_t device, double* flops);
+/* Self-check of the reference-form pair arithmetic: the correctly rounded
+ * sqrt(a) and 1 / (a sqrt(a)) that replace IEEE square root and division in
+ * every FP64 GravityAC pair (Acceleration.cpp:294-317), compared bit for bit
+ * with IEEE sqrt and division on n seeded samples of one input family
+ * (mode 0: a log-uniform over [2^-200, 2^200]; 1: square roots within
+ * 2^-13 ulp of a midpoint; 2: squared distances in a 100 AU box; 3:
+ * reciprocals within 2^-12 ulp of a midpoint from approximations up to 300
+ * ulps off; 4: log-uniform reciprocals from such approximations; 5: square
+ * roots and reciprocals next to powers of two).
+ * result[0] = samples whose fast path disagrees (0 when correct),
+ * result[1] = samples the fast path hands to IEEE sqrt and division,
+ * result[2] = the first disagreeing sample's index, or -1. */
+int sol_check_pair_math(int32_t device, int32_t mode, int64_t n, uint64_t seed, int64_t result[3]);
 /* Number of kernels this library launched since load. */
 int sol_kernel_launch_count(int64_t* count);
 /* The CUDA stream (cudaStream_t) every kernel of this context is launched on. */

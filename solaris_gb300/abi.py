@@ -193,6 +193,7 @@ def _declare(lib):
                                        C.POINTER(C.c_int32)]),
         "sol_integrals": (C.c_int, [P, _PF64, _PF64]),
         "sol_measure_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
+        "sol_check_pair_math": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
         "sol_kernel_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
         "sol_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
         "sol_bench_force": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
@@ -260,7 +261,8 @@ def exported_names():
         "sol_get_driver_vectors", "sol_get_side_buffers", "sol_bench_stages", "sol_output_open",
         "sol_output_save_phases", "sol_output_save_integrals", "sol_output_flush", "sol_output_close",
         "sol_format_phases_record", "sol_format_integrals_record", "sol_phases_from_elements",
-        "sol_handle_events", "sol_get_bodies", "sol_write_affairs", "sol_run_until", "sol_flush_smallest", "sol_get_step_start"]
+        "sol_handle_events", "sol_get_bodies", "sol_write_affairs", "sol_run_until", "sol_flush_smallest", "sol_get_step_start",
+        "sol_check_pair_math"]
 
 
 def load_library(path: str | None = None):

@@ -1,5 +1,6 @@
-// Event predicates, integrals and the FP64 throughput microbenchmark.
-#include "sol_internal.cuh"
+// Event predicates, integrals, the FP64 throughput microbenchmark and the
+// self-check of the reference-form pair arithmetic.
+#include "sol_crmath.cuh"
 
 namespace {
 
@@ -91,6 +92,88 @@ __global__ void k_dfma_peak(double seed, double b, double* out, int iters) {
   if (s == -12345.0) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Self-check of sol_ref_rinv3 (correctly rounded sqrt and 1 / (a sqrt a))
+// and of its reciprocal step against IEEE sqrt and division, on seeded
+// samples (splitmix64 of the sample index):
+//   0: a log-uniform over [2^-200, 2^200];
+//   1: a = (1 + i 2^-25 + (i^2 +- 1) 2^-52) 4^k, whose square root lies
+//      i 2^-27 ulp from a midpoint (i < 11,000): both sides of the 2^-16 band;
+//   2: a = squared distance of two positions uniform in a 100 AU box;
+//   3: d = (1 - x 2^-53) 2^s (x odd < 2^21), whose reciprocal lies x^2 2^-54
+//      ulp from a midpoint, from approximations up to 300 ulps off;
+//   4: d log-uniform over [2^-200, 2^200], approximations up to 300 ulps off;
+//   5: a = (1 + u, 2 +- u or 4 - u) 4^k, u log-uniform over [2^-60, 2^-10]:
+//      square roots and reciprocals next to powers of two.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double unit_double(unsigned long long h) { return (double)(h >> 11) * 0x1.0p-53; }
+
+__global__ void k_check_rinv3(int mode, long long n, unsigned long long seed, unsigned long long* counts,
+                              long long* first) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += stride) {
+    const unsigned long long h1 = mix64(seed ^ mix64((unsigned long long)s));
+    const unsigned long long h2 = mix64(h1);
+    bool ok = true, bad = false;
+    if (mode <= 2 || mode == 5) {
+      double a;
+      if (mode == 5) {
+        const double u = unit_double(h1) * __longlong_as_double((long long)(1023 - 10 - (long long)(h2 % 51)) << 52);
+        const int w = (int)((h2 >> 32) % 4);
+        const double m = w == 0 ? 1.0 + u : w == 1 ? 2.0 + u : w == 2 ? 2.0 - u : 4.0 - u;
+        const long long k = (long long)((h2 >> 40) % 201) - 100;
+        a = m * __longlong_as_double((1023 + 2 * k) << 52);
+      } else if (mode == 0) {
+        const long long E = 1023 - 200 + (long long)(h2 % 401);
+        a = __longlong_as_double((E << 52) | (long long)(h1 & 0xFFFFFFFFFFFFFull));
+      } else if (mode == 1) {
+        const long long i = 1 + (long long)(h1 % 11000);
+        const long long t = i * i + (((h1 >> 40) & 1) ? 1 : -1);
+        const long long k = (long long)(h2 % 201) - 100;
+        a = __longlong_as_double(((1023 + 2 * k) << 52) | ((i << 27) + t));
+      } else {
+        const unsigned long long h3 = mix64(h2), h4 = mix64(h3), h5 = mix64(h4), h6 = mix64(h5);
+        const double dx = 100.0 * unit_double(h1) - 100.0 * unit_double(h2);
+        const double dy = 100.0 * unit_double(h3) - 100.0 * unit_double(h4);
+        const double dz = 100.0 * unit_double(h5) - 100.0 * unit_double(h6);
+        a = dx * dx + dy * dy + dz * dz;
+      }
+      double r, rm3;
+      ok = sol_ref_rinv3_fast(a, r, rm3);
+      if (ok) {
+        const double rr = __dsqrt_rn(a);
+        const double w = __ddiv_rn(1.0, a * rr);
+        bad = (__double_as_longlong(r) != __double_as_longlong(rr)) ||
+              (__double_as_longlong(rm3) != __double_as_longlong(w));
+      }
+    } else {
+      double d;
+      if (mode == 3) {
+        const long long x = (long long)((h1 % (1ull << 21)) | 1ull);
+        const long long sc = (long long)(h2 % 201) - 100;
+        d = __longlong_as_double(((1022 + sc) << 52) | ((1LL << 52) - x));
+      } else {
+        const long long E = 1023 - 200 + (long long)(h2 % 401);
+        d = __longlong_as_double((E << 52) | (long long)(h1 & 0xFFFFFFFFFFFFFull));
+      }
+      const double w = __ddiv_rn(1.0, d);
+      const long long zb = __double_as_longlong(w) + ((long long)((h2 >> 20) % 601) - 300);
+      const long long wb = solcr::rcp_from_approx(d, zb, ok);
+      bad = ok && (wb != __double_as_longlong(w));
+    }
+    if (!ok) atomicAdd(&counts[1], 1ull);
+    if (bad) {
+      atomicAdd(&counts[0], 1ull);
+      atomicMin(reinterpret_cast<unsigned long long*>(first), (unsigned long long)s);
+    }
+  }
+}
+
 }  // namespace
 
 int sol_events_launch(sol_ctx* c, const double* d_y0, double ej, double hc, double cf, sol_event* d_out,
@@ -139,4 +222,30 @@ int sol_fp64_peak_launch(int device, double* flops) {
   const double fmas = (double)threads * blocks * 8.0 * iters;
   *flops = 2.0 * fmas / (best * 1e-3);
   return SOL_OK;
+}
+
+int sol_check_pair_math_launch(int device, int mode, long long n, unsigned long long seed, long long* result) {
+  SOL_CUDA(cudaSetDevice(device));
+  int nsm = 0;
+  SOL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+  unsigned long long* d = nullptr;
+  SOL_CUDA(cudaMalloc(&d, 3 * sizeof(unsigned long long)));
+  const unsigned long long init[3] = {0ull, 0ull, ~0ull};
+  int rc = SOL_OK;
+  if (cudaMemcpy(d, init, sizeof(init), cudaMemcpyHostToDevice) != cudaSuccess) rc = SOL_ERR_CUDA;
+  if (rc == SOL_OK) {
+    k_check_rinv3<<<nsm * 8, 256>>>(mode, n, seed, d, reinterpret_cast<long long*>(d + 2));
+    SOL_LAUNCHED();
+    unsigned long long h[3];
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = SOL_ERR_CUDA;
+    else {
+      result[0] = (long long)h[0];
+      result[1] = (long long)h[1];
+      result[2] = h[2] == ~0ull ? -1 : (long long)h[2];
+    }
+  }
+  cudaFree(d);
+  if (rc != SOL_OK) sol_set_error("pair arithmetic self-check: CUDA error");
+  return rc;
 }

@@ -17,7 +17,7 @@
 #include <vector>
 
 #include "sol_internal.cuh"
-#include "sol_pair.cuh"
+#include "sol_crmath.cuh"
 
 namespace {
 
@@ -72,8 +72,9 @@ __device__ void ens_force(const EnsSys& S, const double* __restrict__ m, const d
     if (i >= 1) {
       const double x = yin[6 * i], y = yin[6 * i + 1], z = yin[6 * i + 2];
       const double r2 = x * x + y * y + z * z;
-      const double r = __dsqrt_rn(r2);
-      rm3[i] = __ddiv_rn(1.0, r2 * r);
+      double r, rm3i;
+      sol_ref_rinv3(r2, r, rm3i);
+      rm3[i] = rm3i;
     } else {
       rm3[0] = 0.0;
     }
@@ -147,8 +148,8 @@ __device__ void ens_force(const EnsSys& S, const double* __restrict__ m, const d
         if (j == i) continue;
         const double xij = tx[j] - xi, yij = ty[j] - yi, zij = tz[j] - zi;
         const double rij2 = xij * xij + yij * yij + zij * zij;
-        const double rij = __dsqrt_rn(rij2);
-        const double rijm3 = __ddiv_rn(1.0, rij2 * rij);
+        double rij, rijm3;
+        sol_ref_rinv3(rij2, rij, rijm3);
         const double gm = tg[j];
         ax += gm * (xij * rijm3 - tpx[j]);
         ay += gm * (yij * rijm3 - tpy[j]);

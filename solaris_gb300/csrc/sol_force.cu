@@ -17,7 +17,7 @@
 #include <mutex>
 
 #include "sol_internal.cuh"
-#include "sol_pair.cuh"
+#include "sol_crmath.cuh"
 
 namespace {
 
@@ -51,8 +51,8 @@ __global__ void k_prepass(ForceCtx fc, const double* __restrict__ y, int split) 
         if (!fc.barycentric) {
           // Acceleration.cpp:259-261
           double r2 = x * x + yy * yy + z * z;
-          double r = __dsqrt_rn(r2);
-          rm3 = __ddiv_rn(1.0, r2 * r);
+          double r;
+          sol_ref_rinv3(r2, r, rm3);
           fc.rm3[j] = rm3;
         }
         gm = SOL_GAUSS2 * fc.mass[j];
@@ -143,8 +143,8 @@ __device__ __forceinline__ void pair_fp64(const TileSmem<7>& sm, int st, int jj,
     double yij = sm.v[st][SY][jj] - yi;
     double zij = sm.v[st][SZ][jj] - zi;
     double rij2 = xij * xij + yij * yij + zij * zij;
-    double rij = __dsqrt_rn(rij2);
-    double rijm3 = __ddiv_rn(1.0, rij2 * rij);
+    double rij, rijm3;
+    sol_ref_rinv3(rij2, rij, rijm3);
     long long rb = __double_as_longlong(rij);
     if (rb < rminb) {
       rminb = rb;
@@ -420,8 +420,8 @@ __global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const doubl
             const double yij = yj - sink_pos[s][1];
             const double zij = zj - sink_pos[s][2];
             const double rij2 = xij * xij + yij * yij + zij * zij;
-            const double rij = __dsqrt_rn(rij2);
-            const double rijm3 = __ddiv_rn(1.0, rij2 * rij);
+            double rij, rijm3;
+            sol_ref_rinv3(rij2, rij, rijm3);
             const long long rb = __double_as_longlong(rij);
             if (rb < rminb[s]) {
               rminb[s] = rb;
@@ -490,6 +490,179 @@ __global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const doubl
   a[2] += acc[2 * kFewSinks + s];
   fc.nn_idx[i] = bj;
   fc.nn_dist[i] = bj >= 0 ? __longlong_as_double(best) : 0.0;
+  add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
+  out[0] = yv[3];
+  out[1] = yv[4];
+  out[2] = yv[5];
+  out[3] = a[0];
+  out[4] = a[1];
+  out[5] = a[2];
+}
+
+// ---- FP64 GravityAC, 32 sinks per CTA ----------------------------------------
+// The FP64 pipe spends 64 cycles on every warp instruction however many of
+// its lanes are active, so the in-order sums of k_gravity_ac_few (12 of 32
+// lanes) cost almost a third of its pair work.  Here a CTA takes 32 sinks and
+// alternates two phases per round of kWideTile sources:
+//  A. every thread computes one source's terms against 16 of the 32 sinks
+//     (the reference arithmetic, Acceleration.cpp:294-317) into a shared row;
+//     the nearest-neighbour candidates of each sink are reduced across the
+//     warp with three 32-bit minimum reductions (high word, low word, index)
+//     and kept by one lane of the warp;
+//  B. three full warps -- warp c for component c, lane s for sink s -- add the
+//     round's terms in ascending source order.
+// The sums are the reference's sequential sums (bit-identical to
+// k_gravity_ac_few); a sum costs 3 FP64 warp instructions per round.  A CTA
+// takes spc <= 32 sinks: the host picks spc so that the CTAs fill whole
+// waves of two per SM (the per-round cost 0.625 spc + 3 FP64 warp
+// instructions per source, times the waves, is smallest).
+constexpr int kWideSinks = 32;
+constexpr int kWideWarps = 8;                          // 16 per SM: four per sub-partition
+constexpr int kWideTile = kWideWarps * 32 / 2;         // 128 sources per round
+constexpr int kWideRow = 3 * kWideSinks + 1;           // doubles per source row (odd: conflict-free columns)
+constexpr size_t kWideSmem = sizeof(double) * kWideTile * kWideRow;  // 99,328 bytes: two CTAs per SM
+constexpr int kMaxDevices = 64;
+// below this many sinks per CTA the 4-sink kernel's finer grid wins
+constexpr int kWideMinSinks = 12;
+
+__global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx fc, const double* __restrict__ y,
+                                                                        double* __restrict__ dydt, TimeSpec ts,
+                                                                        uint32_t flags, int spc) {
+  extern __shared__ __align__(16) double wide_terms[];  // [kWideTile][kWideRow]
+  __shared__ double sink_pos[kWideSinks][3];
+  __shared__ int sink_ns[kWideSinks];
+  __shared__ double acc[3][kWideSinks];
+  __shared__ unsigned long long nn_key[kWideWarps][kWideSinks];
+  __shared__ int nn_j[kWideWarps][kWideSinks];
+  const Classes& c = fc.cls;
+  const int n = c.n;
+  const int i0 = blockIdx.x * spc;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < kWideSinks) {
+    const int i = i0 + threadIdx.x;
+    const bool live = i < n && i >= 1 && threadIdx.x < spc;
+    sink_ns[threadIdx.x] = live ? ((fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm) : 0;
+    for (int k = 0; k < 3; ++k) sink_pos[threadIdx.x][k] = i < n ? y[6 * i + k] : 0.0;
+  }
+  __syncthreads();
+  int ns_cta = 0;
+  for (int s = 0; s < kWideSinks; ++s) ns_cta = max(ns_cta, sink_ns[s]);
+  const int rounds = (ns_cta + kWideTile - 1) / kWideTile;
+  const double* src = fc.src;
+  const int np = fc.npad;
+
+  // lane s of every warp: the first minimum of sink h ceil(spc/2) + s
+  // (h = warp / 4) over this warp's sources
+  unsigned long long best = (unsigned long long)__double_as_longlong(1.0e10);
+  int best_j = -1;
+  // phase-B lanes: component warp, sink lane
+  const int b_i = i0 + lane;
+  const int b_ns = sink_ns[lane];
+  double a_sum = 0.0;
+
+  for (int r = 0; r < rounds; ++r) {
+    // ---- phase A ----
+    {
+      const int p = threadIdx.x % kWideTile;
+      const int half = (spc + 1) >> 1;
+      const int s0 = (threadIdx.x / kWideTile) * half;
+      const int s1 = min(s0 + half, spc);
+      const int j = r * kWideTile + p;
+      const bool jin = j < ns_cta;
+      double xj = 0, yj = 0, zj = 0, gm = 0, px = 0, py = 0, pz = 0;
+      if (jin) {
+        xj = src[SX * np + j];
+        yj = src[SY * np + j];
+        zj = src[SZ * np + j];
+        gm = src[SGM * np + j];
+        px = src[SPX * np + j];
+        py = src[SPY * np + j];
+        pz = src[SPZ * np + j];
+      }
+      double* row = wide_terms + (size_t)p * kWideRow;
+#pragma unroll 2
+      for (int s = s0; s < s1; ++s) {
+        unsigned long long key = ~0ull;
+        if (jin && j >= 1 && j < sink_ns[s] && j != i0 + s) {
+          const double xij = xj - sink_pos[s][0];
+          const double yij = yj - sink_pos[s][1];
+          const double zij = zj - sink_pos[s][2];
+          const double rij2 = xij * xij + yij * yij + zij * zij;
+          double rij, rijm3;
+          sol_ref_rinv3(rij2, rij, rijm3);
+          key = (unsigned long long)__double_as_longlong(rij);
+          row[0 * kWideSinks + s] = gm * (xij * rijm3 - px);
+          row[1 * kWideSinks + s] = gm * (yij * rijm3 - py);
+          row[2 * kWideSinks + s] = gm * (zij * rijm3 - pz);
+        }
+        // the warp's smallest (rij, j): high word, then low word, then index
+        const unsigned hi = (unsigned)(key >> 32);
+        const unsigned mhi = __reduce_min_sync(0xFFFFFFFFu, hi);
+        const unsigned lo = (hi == mhi) ? (unsigned)key : 0xFFFFFFFFu;
+        const unsigned mlo = __reduce_min_sync(0xFFFFFFFFu, lo);
+        const unsigned jj = (hi == mhi && (unsigned)key == mlo) ? (unsigned)j : 0xFFFFFFFFu;
+        const unsigned mj = __reduce_min_sync(0xFFFFFFFFu, jj);
+        const unsigned long long mkey = ((unsigned long long)mhi << 32) | mlo;
+        if (lane == s - s0 && mkey < best) {  // later rounds hold larger indices: ties keep the earlier
+          best = mkey;
+          best_j = (int)mj;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- phase B ----
+    if (warp < 3) {
+      const int j0 = r * kWideTile;
+      const int pmax = min(kWideTile, b_ns - j0);
+      const double* col = wide_terms + warp * kWideSinks + lane;
+      for (int p = 0; p < pmax; ++p) {
+        const int j = j0 + p;
+        if (j >= 1 && j != b_i) a_sum += col[(size_t)p * kWideRow];
+      }
+    }
+    __syncthreads();
+  }
+  nn_key[warp][lane] = best;
+  nn_j[warp][lane] = best_j;
+  if (warp < 3) acc[warp][lane] = a_sum;
+  __syncthreads();
+  if (threadIdx.x >= spc) return;
+  const int s = threadIdx.x;
+  const int i = i0 + s;
+  if (i >= n) return;
+  double* out = dydt + 6 * i;
+  if (i == 0) {  // GravityAC :253-254, :266
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    fc.nn_idx[0] = -1;
+    fc.nn_dist[0] = 0.0;
+    return;
+  }
+  const int half = (spc + 1) >> 1;
+  const int w0 = (s / half) * (kWideWarps / 2);
+  const int hl = s % half;
+  unsigned long long bk = nn_key[w0][hl];
+  int bj = nn_j[w0][hl];
+  for (int w = w0 + 1; w < w0 + kWideWarps / 2; ++w) {
+    const unsigned long long k2 = nn_key[w][hl];
+    const int j2 = nn_j[w][hl];
+    if (j2 >= 0 && (bj < 0 || k2 < bk || (k2 == bk && j2 < bj))) {
+      bk = k2;
+      bj = j2;
+    }
+  }
+  const double* yv = y + 6 * i;
+  const double xi = sink_pos[s][0], yi = sink_pos[s][1], zi = sink_pos[s][2];
+  const double mu = SOL_GAUSS2 * (fc.mass[0] + fc.mass[i]);
+  const double rm3i = fc.rm3[i];
+  double a[3];
+  a[0] = -mu * rm3i * xi;  // Kepler term first (:281-283)
+  a[1] = -mu * rm3i * yi;
+  a[2] = -mu * rm3i * zi;
+  a[0] += acc[0][s];
+  a[1] += acc[1][s];
+  a[2] += acc[2][s];
+  fc.nn_idx[i] = bj;
+  fc.nn_dist[i] = bj >= 0 ? __longlong_as_double((long long)bk) : 0.0;
   add_gas_terms(fc, i, yv, eval_time(ts), flags, a);
   out[0] = yv[3];
   out[1] = yv[4];
@@ -938,7 +1111,37 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
   // sinks with fewer sources than one producer tile (a few massive bodies and
   // many light ones) are cheaper with one thread per sink
   if (!split && c->cls.nm + c->cls.n_spl >= kFewTile) {
-    k_gravity_ac_few<<<(c->n + kFewSinks - 1) / kFewSinks, 256, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
+    // per device: the SM count, once the wide kernel's shared-memory size is allowed
+    static int wide_sms[kMaxDevices];
+    const int dev = (c->device >= 0 && c->device < kMaxDevices) ? c->device : 0;
+    if (wide_sms[dev] == 0) {
+      int nsm = 0;
+      SOL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+      SOL_CUDA(cudaFuncSetAttribute(k_gravity_ac_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWideSmem));
+      wide_sms[dev] = nsm;
+    }
+    // sinks per CTA: the fewest whole waves of two CTAs per SM, then the
+    // cheapest of that and the next two wave counts
+    const int slots = 2 * wide_sms[dev];
+    int spc = 0;
+    {
+      const int k0 = (c->n + slots * kWideSinks - 1) / (slots * kWideSinks);
+      double best = 1e300;
+      for (int k = k0; k < k0 + 3; ++k) {
+        const int sp = (c->n + k * slots - 1) / (k * slots);
+        const double cost = k * (0.625 * sp + 3.0);
+        if (cost < best) {
+          best = cost;
+          spc = sp;
+        }
+      }
+    }
+    if (spc >= kWideMinSinks) {
+      k_gravity_ac_wide<<<(c->n + spc - 1) / spc, kWideWarps * 32, kWideSmem, c->stream>>>(fc, d_y, d_dydt, ts,
+                                                                                           flags, spc);
+    } else {
+      k_gravity_ac_few<<<(c->n + kFewSinks - 1) / kFewSinks, 256, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
+    }
     SOL_LAUNCHED();
     return SOL_OK;
   }

@@ -33,7 +33,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "sol_internal.cuh"
+#include "sol_crmath.cuh"
 
 namespace {
 
@@ -319,8 +319,8 @@ __device__ __noinline__ void evaluate(const GroupArgs& P, const View& V, double 
         if (i >= 1) {  // Acceleration.cpp:259-261
           const double x = y[0], yy = y[1], z = y[2];
           const double r2 = x * x + yy * yy + z * z;
-          const double rr = __dsqrt_rn(r2);
-          rm3 = __ddiv_rn(1.0, r2 * rr);
+          double rr;
+          sol_ref_rinv3(r2, rr, rm3);
           if (s >= ns || home) fc.rm3[i] = rm3;
         }
         V.rm3[s] = rm3;
@@ -340,8 +340,8 @@ __device__ __noinline__ void evaluate(const GroupArgs& P, const View& V, double 
         const double yij = yj[1] - yi[1];
         const double zij = yj[2] - yi[2];
         const double rij2 = xij * xij + yij * yij + zij * zij;
-        const double rij = __dsqrt_rn(rij2);
-        const double rijm3 = __ddiv_rn(1.0, rij2 * rij);
+        double rij, rijm3;
+        sol_ref_rinv3(rij2, rij, rijm3);
         V.prb[s * ns + j] = __double_as_longlong(rij);
         V.pp[(0 * nsink + s) * ns + j] = xij * rijm3;
         V.pp[(1 * nsink + s) * ns + j] = yij * rijm3;

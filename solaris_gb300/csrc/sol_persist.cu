@@ -31,7 +31,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "sol_internal.cuh"
+#include "sol_crmath.cuh"
 
 namespace {
 
@@ -112,8 +112,8 @@ __device__ __forceinline__ void own_prepass(const PersistArgs& P, int i, const d
   const double x = y[0], yy = y[1], z = y[2];
   if (i >= 1) {
     const double r2 = x * x + yy * yy + z * z;
-    const double r = __dsqrt_rn(r2);
-    rm3 = __ddiv_rn(1.0, r2 * r);
+    double r;
+    sol_ref_rinv3(r2, r, rm3);
     P.fc.rm3[i] = rm3;
   }
   if (i < P.ns_max) {
@@ -151,8 +151,8 @@ __device__ __forceinline__ void own_force(const PersistArgs& P, int i, const dou
     const double yij = st[1 * kMaxSources + j] - yi;
     const double zij = st[2 * kMaxSources + j] - zi;
     const double rij2 = xij * xij + yij * yij + zij * zij;
-    const double rij = __dsqrt_rn(rij2);
-    const double rijm3 = __ddiv_rn(1.0, rij2 * rij);
+    double rij, rijm3;
+    sol_ref_rinv3(rij2, rij, rijm3);
     const long long rb = __double_as_longlong(rij);
     if (rb < rminb) {
       rminb = rb;

@@ -284,6 +284,16 @@ def fp64_peak_flops(device: int = 0) -> float:
     return float(v.value)
 
 
+def check_pair_math(mode: int, n: int, seed: int = 1, device: int = 0) -> dict:
+    """Self-check of the correctly rounded sqrt / reciprocal of the FP64 pair
+    against IEEE sqrt and division (sol_check_pair_math): mismatches (0 when
+    correct), samples handed to IEEE arithmetic, first mismatching index."""
+    lib = abi.load_library()
+    r = (C.c_int64 * 3)()
+    abi.check(lib, lib.sol_check_pair_math(int(device), int(mode), int(n), int(seed) & (2**64 - 1), r))
+    return {"mismatches": int(r[0]), "slow": int(r[1]), "first": int(r[2])}
+
+
 # -- output files (BinaryFileAdapter record layouts) -------------------------------
 class Output:
     """Phases / integrals files of a context: records appended in the

@@ -117,11 +117,13 @@ def test_full_size_fp64_checksum_and_split_bound():
             assert abs(nds[i] - nd[i]) <= 1e-13 * nd[i]
 
 
-@pytest.mark.parametrize("n", [2, 3, 17, 255, 256, 257, 1000, 4097, 16384, 16385])
+@pytest.mark.parametrize("n", [2, 3, 17, 255, 256, 257, 1000, 4097, 9727, 9728, 9729, 16384, 16385])
 def test_tails_against_oracle(n):
     """Tile tails, tiny systems and the sizes where the kernel choice changes
-    (one thread per sink below one tile of sources; the few-sinks kernels up to
-    16,384 bodies for the split forms), every precision, against the oracle."""
+    (one thread per sink below one tile of sources; the 32-sink FP64 kernel
+    from two CTAs per SM, 9,728 bodies on 152 SMs; the few-sinks kernels up
+    to 16,384 bodies for the split forms), every precision, against the
+    oracle."""
     s = scenarios.config3(seed=5000 + n, n=n)
     o = oracle.Oracle(s)
     ref = o.compute(0.0, s.y0)
@@ -156,6 +158,25 @@ def test_mixed_classes_against_oracle_split():
     assert rel_accel_err(d64, ref).max() <= GAS_RTOL
     for p, dsp in outs.items():
         assert rel_accel_err(dsp, ref).max() <= SPLIT_RTOL, p
+
+
+def test_mixed_classes_wide_fp64():
+    """The 32-sink FP64 kernel with sinks of both source ranges side by side
+    (massive sinks see the super-planetesimals, planetesimals do not), gas
+    drag and migration, against the oracle bit for bit away from the gas
+    bodies."""
+    s = scenarios.mixed_gas_system(seed=3200, n_spl=260, n_pl=9600, n_tp=300, n_proto=200)
+    assert s.n >= 2 * 152 * 32
+    o = oracle.Oracle(s)
+    ref = o.compute(3.0, s.y0)
+    rm3_o, nn_o, nd_o = o.last_eval()
+    with engine.Context(s) as ctx:
+        d64, rm3, nn, nd = ctx.accel(3.0, s.y0)
+    g = gas_bodies(s)
+    assert np.array_equal(bits(d64.reshape(-1, 6)[~g]), bits(ref.reshape(-1, 6)[~g]))
+    assert rel_accel_err(d64, ref).max() <= GAS_RTOL
+    assert np.array_equal(bits(rm3), bits(rm3_o))
+    assert np.array_equal(nn, nn_o) and np.array_equal(bits(nd), bits(nd_o))
 
 
 def test_eval_flags_and_stale_buffers():
