@@ -391,10 +391,11 @@ def main():
                   ("fp64", abi.PRECISION_FP64, 2))}
     peak = engine.fp64_peak_flops(local)  # FLOP/s, FMA = 2
     peak_ops = peak / 2.0                 # FP64 pipe instructions per second
-    # FP64 instructions per pair each form issues; the reference form: 20 in the
-    # pair (correctly rounded sqrt and reciprocal by one FMA remainder each) and
-    # 3 in-order additions at 31 sinks per CTA (3 x 32 / 31)
-    fp64_ops = {"split_ff": 3, "split": 16, "fp64": 23}
+    # FP64 instructions per pair each form issues; the reference form: 14 in the
+    # pair (correctly rounded sqrt and reciprocal by one FMA remainder each, the
+    # six term multiplies on the integer pipe) and 3 in-order additions at 31
+    # sinks per CTA (3 x 32 / 31)
+    fp64_ops = {"split_ff": 3, "split": 16, "fp64": 17}
 
     # end to end through the C-ABI: pinned host state in, host state out, every step
     y_host = torch.empty(6 * s.n, dtype=torch.float64, pin_memory=True).numpy()

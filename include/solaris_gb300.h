@@ -471,13 +471,16 @@ int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_type, const 
 int sol_measure_fp64_peak(int32_t device, double* flops);
 /* Self-check of the reference-form pair arithmetic: the correctly rounded
  * sqrt(a) and 1 / (a sqrt(a)) that replace IEEE square root and division in
- * every FP64 GravityAC pair (Acceleration.cpp:294-317), compared bit for bit
- * with IEEE sqrt and division on n seeded samples of one input family
+ * every FP64 GravityAC pair (Acceleration.cpp:294-317), and the integer-pipe
+ * multiply of its terms, compared bit for bit with the FP64 instructions on
+ * n seeded samples of one input family
  * (mode 0: a log-uniform over [2^-200, 2^200]; 1: square roots within
  * 2^-13 ulp of a midpoint; 2: squared distances in a 100 AU box; 3:
  * reciprocals within 2^-12 ulp of a midpoint from approximations up to 300
  * ulps off; 4: log-uniform reciprocals from such approximations; 5: square
- * roots and reciprocals next to powers of two).
+ * roots and reciprocals next to powers of two; 6: the integer-pipe double
+ * multiply of the pair terms against the FP64 instruction, random operands;
+ * 7: the same next to the normalisation boundaries, zeros and squares).
  * result[0] = samples whose fast path disagrees (0 when correct),
  * result[1] = samples the fast path hands to IEEE sqrt and division,
  * result[2] = the first disagreeing sample's index, or -1. */

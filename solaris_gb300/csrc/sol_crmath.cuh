@@ -195,3 +195,70 @@ __device__ __forceinline__ void sol_ref_rinv3(double a, double& rij, double& rij
   if (!sol_ref_rinv3_fast(a, rij, rijm3)) sol_ref_rinv3_slow(a, rij, rijm3);
 }
 
+// ---- IEEE double multiplication on the integer pipe ----------------------------
+// Round-to-nearest-even product of two doubles from 32-bit integer
+// multiplies of the significands (the 106-bit product in three words, the
+// leading 53 bits, guard and sticky bits): the textbook IEEE 754 multiply.
+// It is exact wherever the inputs are finite and normal or zero and the
+// product is normal or zero; ok turns false elsewhere (the caller then takes
+// the FP64 instruction).  A pair's term multiplies move here from the FP64
+// pipe, which binds the reference form, to the integer pipe, which it leaves
+// mostly idle.
+__device__ __forceinline__ double sol_exact_dmul(double a, double b, bool& ok) {
+  const unsigned ah = (unsigned)__double2hiint(a), al = (unsigned)__double2loint(a);
+  const unsigned bh = (unsigned)__double2hiint(b), bl = (unsigned)__double2loint(b);
+  const int ea = (int)((ah >> 20) & 0x7FFu), eb = (int)((bh >> 20) & 0x7FFu);
+  const unsigned sign = (ah ^ bh) & 0x80000000u;
+  const unsigned mah = (ah & 0xFFFFFu) | 0x100000u, mbh = (bh & 0xFFFFFu) | 0x100000u;
+  // Ma Mb in [2^104, 2^106): bits 64.. in t3, 32..63 in w1, 0..31 in w0
+  const unsigned long long t0 = (unsigned long long)al * bl;
+  const unsigned long long t1 = (unsigned long long)mah * bl + (t0 >> 32);
+  const unsigned long long t2 = (unsigned long long)al * mbh + (t1 & 0xFFFFFFFFull);
+  const unsigned long long t3 = (unsigned long long)mah * mbh + (t1 >> 32) + (t2 >> 32);
+  const unsigned w1 = (unsigned)t2, w0 = (unsigned)t0;
+  const int n = (int)(t3 >> 41);  // product >= 2^105: one more place to drop
+  const int s = 20 + n;
+  const unsigned long long m = (t3 << (32 - s)) | (unsigned long long)(w1 >> s);  // the leading 53 bits
+  const unsigned guard = (w1 >> (s - 1)) & 1u;
+  const unsigned sticky = (w1 & ((1u << (s - 1)) - 1u)) | w0;
+  const unsigned long long rnd = guard & ((sticky != 0u) | (unsigned)(m & 1ull));
+  const int e = ea + eb - 1023 + n;
+  const bool za = (ea == 0) & (((ah & 0xFFFFFu) | al) == 0u);
+  const bool zb = (eb == 0) & (((bh & 0xFFFFFu) | bl) == 0u);
+  const bool zero = za | zb;
+  ok = ok && ((ea != 0) | za) && ((eb != 0) | zb) && (ea != 0x7FF) && (eb != 0x7FF) && (zero | ((e >= 1) & (e <= 2045)));
+  // a rounding carry out of the significand moves into the exponent field
+  const unsigned long long bits = zero ? 0ull : ((unsigned long long)e << 52) + (m - (1ull << 52)) + rnd;
+  return __longlong_as_double((long long)(bits | ((unsigned long long)sign << 32)));
+}
+
+// The reference's pair term gm (d rijm3 - p) per component
+// (Acceleration.cpp:306-308), its six multiplications on the integer pipe;
+// bit-identical to the FP64 expression.
+__device__ __forceinline__ void sol_ref_terms(double gm, double rijm3, double dx, double dy, double dz, double px,
+                                              double py, double pz, double& tx, double& ty, double& tz) {
+  bool ok = true;
+  const double ux = sol_exact_dmul(dx, rijm3, ok) - px;
+  const double uy = sol_exact_dmul(dy, rijm3, ok) - py;
+  const double uz = sol_exact_dmul(dz, rijm3, ok) - pz;
+  tx = sol_exact_dmul(gm, ux, ok);
+  ty = sol_exact_dmul(gm, uy, ok);
+  tz = sol_exact_dmul(gm, uz, ok);
+  if (!ok) {
+    tx = gm * (dx * rijm3 - px);
+    ty = gm * (dy * rijm3 - py);
+    tz = gm * (dz * rijm3 - pz);
+  }
+}
+
+// Two independent pairs in one basic block (their dependency chains
+// interleave), the rare IEEE fallbacks after both.
+__device__ __forceinline__ void sol_ref_rinv3_x2(double a0, double a1, double& r0, double& w0, double& r1,
+                                                 double& w1) {
+  const bool ok0 = sol_ref_rinv3_fast(a0, r0, w0);
+  const bool ok1 = sol_ref_rinv3_fast(a1, r1, w1);
+  if (!(ok0 && ok1)) {
+    if (!ok0) sol_ref_rinv3_slow(a0, r0, w0);
+    if (!ok1) sol_ref_rinv3_slow(a1, r1, w1);
+  }
+}

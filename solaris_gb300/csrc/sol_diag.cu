@@ -103,7 +103,11 @@ __global__ void k_dfma_peak(double seed, double b, double* out, int iters) {
 //      ulp from a midpoint, from approximations up to 300 ulps off;
 //   4: d log-uniform over [2^-200, 2^200], approximations up to 300 ulps off;
 //   5: a = (1 + u, 2 +- u or 4 - u) 4^k, u log-uniform over [2^-60, 2^-10]:
-//      square roots and reciprocals next to powers of two.
+//      square roots and reciprocals next to powers of two;
+//   6: the integer-pipe multiply sol_exact_dmul against the FP64 instruction,
+//      random signed operands with exponents over [2^-300, 2^300];
+//   7: the same with significands whose product sits next to 2^104 or 2^106,
+//      zeros and squares.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
   x += 0x9E3779B97F4A7C15ull;
   x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -120,7 +124,33 @@ __global__ void k_check_rinv3(int mode, long long n, unsigned long long seed, un
     const unsigned long long h1 = mix64(seed ^ mix64((unsigned long long)s));
     const unsigned long long h2 = mix64(h1);
     bool ok = true, bad = false;
-    if (mode <= 2 || mode == 5) {
+    if (mode >= 6) {
+      unsigned long long ea = 1023 - 300 + (h1 >> 52) % 601, eb = 1023 - 300 + (h2 >> 52) % 601;
+      unsigned long long ma = h1 & 0xFFFFFFFFFFFFFull, mb = h2 & 0xFFFFFFFFFFFFFull;
+      if (mode == 7) {
+        const unsigned w = (unsigned)((h1 >> 44) & 3);
+        if (w == 0) {
+          ma |= 0xFFFFFFF000000ull;
+          mb |= 0xFFFFFFF000000ull;
+        } else if (w == 1) {
+          ma &= 0x0000000FFFFFFull;
+          mb &= 0x00000000FFFFFull;
+        } else if (w == 2) {
+          mb = ma;
+          eb = ea;
+        } else if ((h2 >> 40) & 1) {
+          ma = 0;
+          ea = 0;
+        } else {
+          mb = 0;
+          eb = 0;
+        }
+      }
+      const double a = __longlong_as_double((long long)((ea << 52) | ma | ((h1 & 1ull) << 63)));
+      const double b = __longlong_as_double((long long)((eb << 52) | mb | ((h2 & 1ull) << 63)));
+      const double e = sol_exact_dmul(a, b, ok);
+      bad = ok && (__double_as_longlong(e) != __double_as_longlong(__dmul_rn(a, b)));
+    } else if (mode <= 2 || mode == 5) {
       double a;
       if (mode == 5) {
         const double u = unit_double(h1) * __longlong_as_double((long long)(1023 - 10 - (long long)(h2 % 51)) << 52);

@@ -144,16 +144,32 @@ __device__ void ens_force(const EnsSys& S, const double* __restrict__ m, const d
     double a0 = -mu * rm3[i] * xi, a1 = -mu * rm3[i] * yi, a2 = -mu * rm3[i] * zi;
     if constexpr (PREC == SOL_PRECISION_FP64) {
       double ax = 0.0, ay = 0.0, az = 0.0;
-      for (int j = 1; j < ns; j++) {
-        if (j == i) continue;
-        const double xij = tx[j] - xi, yij = ty[j] - yi, zij = tz[j] - zi;
-        const double rij2 = xij * xij + yij * yij + zij * zij;
-        double rij, rijm3;
-        sol_ref_rinv3(rij2, rij, rijm3);
-        const double gm = tg[j];
-        ax += gm * (xij * rijm3 - tpx[j]);
-        ay += gm * (yij * rijm3 - tpy[j]);
-        az += gm * (zij * rijm3 - tpz[j]);
+      // two sources per step (independent chains that interleave), added in
+      // ascending order; an odd last source pairs with itself
+      for (int j = 1; j < ns; j += 2) {
+        const int jb[2] = {j, min(j + 1, ns - 1)};
+        double xij[2], yij[2], zij[2], rij2[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          xij[u] = tx[jb[u]] - xi;
+          yij[u] = ty[jb[u]] - yi;
+          zij[u] = tz[jb[u]] - zi;
+          const double q = xij[u] * xij[u] + yij[u] * yij[u] + zij[u] * zij[u];
+          rij2[u] = jb[u] != i ? q : 1.0;
+        }
+        double rij[2], rijm3[2];
+        sol_ref_rinv3_x2(rij2[0], rij2[1], rij[0], rijm3[0], rij[1], rijm3[1]);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          double t0, t1, t2;
+          const int q = jb[u];
+          sol_ref_terms(tg[q], rijm3[u], xij[u], yij[u], zij[u], tpx[q], tpy[q], tpz[q], t0, t1, t2);
+          if (q != i && (u == 0 || jb[1] != jb[0])) {
+            ax += t0;
+            ay += t1;
+            az += t2;
+          }
+        }
       }
       a0 += ax;
       a1 += ay;

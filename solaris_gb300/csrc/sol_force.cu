@@ -412,24 +412,36 @@ __global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const doubl
         const double gm = src[SGM * np + j], px = src[SPX * np + j], py = src[SPY * np + j],
                      pz = src[SPZ * np + j];
         double* out = &terms[r & 1][p][0];
+        // two sinks per step, branch-free up to the stores (their chains interleave)
 #pragma unroll
-        for (int s = 0; s < kFewSinks; ++s) {
-          const int i = i0 + s;
-          if (j >= 1 && j < sink_ns[s] && j != i) {
-            const double xij = xj - sink_pos[s][0];
-            const double yij = yj - sink_pos[s][1];
-            const double zij = zj - sink_pos[s][2];
-            const double rij2 = xij * xij + yij * yij + zij * zij;
-            double rij, rijm3;
-            sol_ref_rinv3(rij2, rij, rijm3);
-            const long long rb = __double_as_longlong(rij);
-            if (rb < rminb[s]) {
-              rminb[s] = rb;
-              nn[s] = j;
+        for (int s = 0; s < kFewSinks; s += 2) {
+          double xij[2], yij[2], zij[2], rij2[2];
+          bool valid[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            valid[u] = j >= 1 && j < sink_ns[s + u] && j != i0 + s + u;
+            xij[u] = xj - sink_pos[s + u][0];
+            yij[u] = yj - sink_pos[s + u][1];
+            zij[u] = zj - sink_pos[s + u][2];
+            const double q = xij[u] * xij[u] + yij[u] * yij[u] + zij[u] * zij[u];
+            rij2[u] = valid[u] ? q : 1.0;
+          }
+          double rij[2], rijm3[2];
+          sol_ref_rinv3_x2(rij2[0], rij2[1], rij[0], rijm3[0], rij[1], rijm3[1]);
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            double tx, ty, tz;
+            sol_ref_terms(gm, rijm3[u], xij[u], yij[u], zij[u], px, py, pz, tx, ty, tz);
+            if (valid[u]) {
+              const long long rb = __double_as_longlong(rij[u]);
+              if (rb < rminb[s + u]) {
+                rminb[s + u] = rb;
+                nn[s + u] = j;
+              }
+              out[0 * kFewSinks + s + u] = tx;
+              out[1 * kFewSinks + s + u] = ty;
+              out[2 * kFewSinks + s + u] = tz;
             }
-            out[0 * kFewSinks + s] = gm * (xij * rijm3 - px);
-            out[1 * kFewSinks + s] = gm * (yij * rijm3 - py);
-            out[2 * kFewSinks + s] = gm * (zij * rijm3 - pz);
           }
         }
       }
@@ -514,7 +526,7 @@ __global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const doubl
 // The sums are the reference's sequential sums (bit-identical to
 // k_gravity_ac_few); a sum costs 3 FP64 warp instructions per round.  A CTA
 // takes spc <= 32 sinks: the host picks spc so that the CTAs fill whole
-// waves of two per SM (the per-round cost 0.625 spc + 3 FP64 warp
+// waves of two per SM (the per-round cost 14/32 spc + 3 FP64 warp
 // instructions per source, times the waves, is smallest).
 constexpr int kWideSinks = 32;
 constexpr int kWideWarps = 8;                          // 16 per SM: four per sub-partition
@@ -524,6 +536,56 @@ constexpr size_t kWideSmem = sizeof(double) * kWideTile * kWideRow;  // 99,328 b
 constexpr int kMaxDevices = 64;
 // below this many sinks per CTA the 4-sink kernel's finer grid wins
 constexpr int kWideMinSinks = 12;
+
+// Phase A of k_gravity_ac_wide for NU consecutive sinks from s: the pair
+// terms into the shared row, the warp's nearest-neighbour candidate per sink.
+template <int NU>
+__device__ __forceinline__ void wide_sinks(int s, int s0, int j, bool jin, int i0, int lane, double xj, double yj,
+                                           double zj, double gm, double px, double py, double pz,
+                                           const double (*sink_pos)[3], const int* sink_ns, double* row,
+                                           unsigned long long& best, int& best_j) {
+  double xij[NU], yij[NU], zij[NU], rij2[NU], rij[NU], rijm3[NU];
+  bool valid[NU];
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    valid[u] = jin && j >= 1 && j < sink_ns[s + u] && j != i0 + s + u;
+    xij[u] = xj - sink_pos[s + u][0];
+    yij[u] = yj - sink_pos[s + u][1];
+    zij[u] = zj - sink_pos[s + u][2];
+    const double q = xij[u] * xij[u] + yij[u] * yij[u] + zij[u] * zij[u];
+    rij2[u] = valid[u] ? q : 1.0;
+  }
+  if constexpr (NU == 2)
+    sol_ref_rinv3_x2(rij2[0], rij2[1], rij[0], rijm3[0], rij[1], rijm3[1]);
+  else
+    sol_ref_rinv3(rij2[0], rij[0], rijm3[0]);
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    double tx, ty, tz;
+    sol_ref_terms(gm, rijm3[u], xij[u], yij[u], zij[u], px, py, pz, tx, ty, tz);
+    if (valid[u]) {
+      row[0 * kWideSinks + s + u] = tx;
+      row[1 * kWideSinks + s + u] = ty;
+      row[2 * kWideSinks + s + u] = tz;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    // the warp's smallest (rij, j): high word, then low word, then index
+    const unsigned long long key = valid[u] ? (unsigned long long)__double_as_longlong(rij[u]) : ~0ull;
+    const unsigned hi = (unsigned)(key >> 32);
+    const unsigned mhi = __reduce_min_sync(0xFFFFFFFFu, hi);
+    const unsigned lo = (hi == mhi) ? (unsigned)key : 0xFFFFFFFFu;
+    const unsigned mlo = __reduce_min_sync(0xFFFFFFFFu, lo);
+    const unsigned jj = (hi == mhi && (unsigned)key == mlo) ? (unsigned)j : 0xFFFFFFFFu;
+    const unsigned mj = __reduce_min_sync(0xFFFFFFFFu, jj);
+    const unsigned long long mkey = ((unsigned long long)mhi << 32) | mlo;
+    if (lane == s + u - s0 && mkey < best) {  // later rounds hold larger indices: ties keep the earlier
+      best = mkey;
+      best_j = (int)mj;
+    }
+  }
+}
 
 __global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx fc, const double* __restrict__ y,
                                                                         double* __restrict__ dydt, TimeSpec ts,
@@ -580,33 +642,13 @@ __global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx
         pz = src[SPZ * np + j];
       }
       double* row = wide_terms + (size_t)p * kWideRow;
-#pragma unroll 2
-      for (int s = s0; s < s1; ++s) {
-        unsigned long long key = ~0ull;
-        if (jin && j >= 1 && j < sink_ns[s] && j != i0 + s) {
-          const double xij = xj - sink_pos[s][0];
-          const double yij = yj - sink_pos[s][1];
-          const double zij = zj - sink_pos[s][2];
-          const double rij2 = xij * xij + yij * yij + zij * zij;
-          double rij, rijm3;
-          sol_ref_rinv3(rij2, rij, rijm3);
-          key = (unsigned long long)__double_as_longlong(rij);
-          row[0 * kWideSinks + s] = gm * (xij * rijm3 - px);
-          row[1 * kWideSinks + s] = gm * (yij * rijm3 - py);
-          row[2 * kWideSinks + s] = gm * (zij * rijm3 - pz);
-        }
-        // the warp's smallest (rij, j): high word, then low word, then index
-        const unsigned hi = (unsigned)(key >> 32);
-        const unsigned mhi = __reduce_min_sync(0xFFFFFFFFu, hi);
-        const unsigned lo = (hi == mhi) ? (unsigned)key : 0xFFFFFFFFu;
-        const unsigned mlo = __reduce_min_sync(0xFFFFFFFFu, lo);
-        const unsigned jj = (hi == mhi && (unsigned)key == mlo) ? (unsigned)j : 0xFFFFFFFFu;
-        const unsigned mj = __reduce_min_sync(0xFFFFFFFFu, jj);
-        const unsigned long long mkey = ((unsigned long long)mhi << 32) | mlo;
-        if (lane == s - s0 && mkey < best) {  // later rounds hold larger indices: ties keep the earlier
-          best = mkey;
-          best_j = (int)mj;
-        }
+      // two sinks per step, branch-free up to the stores, so that their
+      // dependency chains interleave; an odd last sink takes a step alone
+      for (int s = s0; s < s1; s += 2) {
+        if (s + 1 < s1)
+          wide_sinks<2>(s, s0, j, jin, i0, lane, xj, yj, zj, gm, px, py, pz, sink_pos, sink_ns, row, best, best_j);
+        else
+          wide_sinks<1>(s, s0, j, jin, i0, lane, xj, yj, zj, gm, px, py, pz, sink_pos, sink_ns, row, best, best_j);
       }
     }
     __syncthreads();
@@ -1129,7 +1171,7 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
       double best = 1e300;
       for (int k = k0; k < k0 + 3; ++k) {
         const int sp = (c->n + k * slots - 1) / (k * slots);
-        const double cost = k * (0.625 * sp + 3.0);
+        const double cost = k * (0.4375 * sp + 3.0);
         if (cost < best) {
           best = cost;
           spc = sp;

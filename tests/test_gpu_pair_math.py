@@ -1,6 +1,7 @@
 """The correctly rounded square root and reciprocal of the FP64 pair
 (sol_crmath.cuh: remainders by FMA, rounding decided from the measured
-distance to the neighbouring doubles) against IEEE sqrt and division,
+distance to the neighbouring doubles) against IEEE sqrt and division, and
+the integer-pipe multiply of the pair terms against the FP64 instruction,
 bit for bit, on seeded sample families (sol_check_pair_math)."""
 import pytest
 
@@ -18,6 +19,8 @@ N = 1 << 28
     (3, 0.3),    # reciprocals x^2 2^-54 ulp from a midpoint (x < 2^19: inside the band), approximations 300 ulps off
     (4, 2e-4),   # log-uniform reciprocals, approximations 300 ulps off
     (5, 0.4),    # square roots and reciprocals next to powers of two (results on a power of two go the IEEE way)
+    (6, 0.0),    # integer-pipe multiply, random operands
+    (7, 0.0),    # integer-pipe multiply next to the normalisation boundaries, zeros, squares
 ])
 def test_pair_math_matches_ieee(mode, max_slow):
     r = engine.check_pair_math(mode, N, seed=1000 + mode)
