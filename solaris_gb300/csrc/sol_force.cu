@@ -514,80 +514,70 @@ __global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const doubl
 // ---- FP64 GravityAC, 32 sinks per CTA ----------------------------------------
 // The FP64 pipe spends 64 cycles on every warp instruction however many of
 // its lanes are active, so the in-order sums of k_gravity_ac_few (12 of 32
-// lanes) cost almost a third of its pair work.  Here a CTA takes 32 sinks and
-// alternates two phases per round of kWideTile sources:
-//  A. every thread computes one source's terms against 16 of the 32 sinks
-//     (the reference arithmetic, Acceleration.cpp:294-317) into a shared row;
-//     the nearest-neighbour candidates of each sink are reduced across the
-//     warp with three 32-bit minimum reductions (high word, low word, index)
-//     and kept by one lane of the warp;
+// lanes) cost almost a third of its pair work.  Here a CTA takes up to 32
+// sinks and alternates two phases per round of kWideTile sources:
+//  A. every thread computes one source's terms against a quarter of the
+//     sinks (the reference arithmetic, Acceleration.cpp:294-317) into a
+//     shared row; the nearest-neighbour candidates of each sink are reduced
+//     across the warp with three 32-bit minimum reductions (high word, low
+//     word, index) and kept by one lane of the warp;
 //  B. three full warps -- warp c for component c, lane s for sink s -- add the
 //     round's terms in ascending source order.
 // The sums are the reference's sequential sums (bit-identical to
 // k_gravity_ac_few); a sum costs 3 FP64 warp instructions per round.  A CTA
 // takes spc <= 32 sinks: the host picks spc so that the CTAs fill whole
-// waves of two per SM (the per-round cost 14/32 spc + 3 FP64 warp
-// instructions per source, times the waves, is smallest).
+// waves of three per SM (the per-round cost 14/32 spc + 3 FP64 warp
+// instructions per source, times the waves, is smallest).  A 64-source tile
+// (49.7 KB) and 85 registers give three CTAs, 24 warps, per SM: measured at
+// 65,536 bodies 151 ms, against 157 ms with four CTAs per SM (64 registers,
+// spilling) and 169 ms with a 128-source tile and two.
 constexpr int kWideSinks = 32;
-constexpr int kWideWarps = 8;                          // 16 per SM: four per sub-partition
-constexpr int kWideTile = kWideWarps * 32 / 2;         // 128 sources per round
+constexpr int kWideWarps = 8;
+constexpr int kWideCtasPerSm = 3;                      // 24 warps per SM: six per sub-partition
+constexpr int kWideTile = 64;                          // sources per round
+constexpr int kWideGroups = kWideWarps * 32 / kWideTile;  // sink quarters: thread = (quarter, source)
 constexpr int kWideRow = 3 * kWideSinks + 1;           // doubles per source row (odd: conflict-free columns)
-constexpr size_t kWideSmem = sizeof(double) * kWideTile * kWideRow;  // 99,328 bytes: two CTAs per SM
+constexpr size_t kWideSmem = sizeof(double) * kWideTile * kWideRow;  // 49,664 bytes
 constexpr int kMaxDevices = 64;
-// below this many sinks per CTA the 4-sink kernel's finer grid wins
-constexpr int kWideMinSinks = 12;
+// below this many sinks per CTA the 4-sink kernel's finer grid wins (measured)
+constexpr int kWideMinSinks = 6;
 
-// Phase A of k_gravity_ac_wide for NU consecutive sinks from s: the pair
-// terms into the shared row, the warp's nearest-neighbour candidate per sink.
-template <int NU>
-__device__ __forceinline__ void wide_sinks(int s, int s0, int j, bool jin, int i0, int lane, double xj, double yj,
-                                           double zj, double gm, double px, double py, double pz,
-                                           const double (*sink_pos)[3], const int* sink_ns, double* row,
-                                           unsigned long long& best, int& best_j) {
-  double xij[NU], yij[NU], zij[NU], rij2[NU], rij[NU], rijm3[NU];
-  bool valid[NU];
-#pragma unroll
-  for (int u = 0; u < NU; ++u) {
-    valid[u] = jin && j >= 1 && j < sink_ns[s + u] && j != i0 + s + u;
-    xij[u] = xj - sink_pos[s + u][0];
-    yij[u] = yj - sink_pos[s + u][1];
-    zij[u] = zj - sink_pos[s + u][2];
-    const double q = xij[u] * xij[u] + yij[u] * yij[u] + zij[u] * zij[u];
-    rij2[u] = valid[u] ? q : 1.0;
+// Phase A of k_gravity_ac_wide for sink s: the pair term into the shared
+// row, the warp's nearest-neighbour candidate.
+__device__ __forceinline__ void wide_sink(int s, int s0, int j, bool jin, int i0, int lane, double xj, double yj,
+                                          double zj, double gm, double px, double py, double pz,
+                                          const double (*sink_pos)[3], const int* sink_ns, double* row,
+                                          unsigned long long& best, int& best_j) {
+  const bool valid = jin && j >= 1 && j < sink_ns[s] && j != i0 + s;
+  const double xij = xj - sink_pos[s][0];
+  const double yij = yj - sink_pos[s][1];
+  const double zij = zj - sink_pos[s][2];
+  const double q = xij * xij + yij * yij + zij * zij;
+  double rij, rijm3;
+  sol_ref_rinv3(valid ? q : 1.0, rij, rijm3);
+  double tx, ty, tz;
+  sol_ref_terms(gm, rijm3, xij, yij, zij, px, py, pz, tx, ty, tz);
+  if (valid) {
+    row[0 * kWideSinks + s] = tx;
+    row[1 * kWideSinks + s] = ty;
+    row[2 * kWideSinks + s] = tz;
   }
-  if constexpr (NU == 2)
-    sol_ref_rinv3_x2(rij2[0], rij2[1], rij[0], rijm3[0], rij[1], rijm3[1]);
-  else
-    sol_ref_rinv3(rij2[0], rij[0], rijm3[0]);
-#pragma unroll
-  for (int u = 0; u < NU; ++u) {
-    double tx, ty, tz;
-    sol_ref_terms(gm, rijm3[u], xij[u], yij[u], zij[u], px, py, pz, tx, ty, tz);
-    if (valid[u]) {
-      row[0 * kWideSinks + s + u] = tx;
-      row[1 * kWideSinks + s + u] = ty;
-      row[2 * kWideSinks + s + u] = tz;
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < NU; ++u) {
-    // the warp's smallest (rij, j): high word, then low word, then index
-    const unsigned long long key = valid[u] ? (unsigned long long)__double_as_longlong(rij[u]) : ~0ull;
-    const unsigned hi = (unsigned)(key >> 32);
-    const unsigned mhi = __reduce_min_sync(0xFFFFFFFFu, hi);
-    const unsigned lo = (hi == mhi) ? (unsigned)key : 0xFFFFFFFFu;
-    const unsigned mlo = __reduce_min_sync(0xFFFFFFFFu, lo);
-    const unsigned jj = (hi == mhi && (unsigned)key == mlo) ? (unsigned)j : 0xFFFFFFFFu;
-    const unsigned mj = __reduce_min_sync(0xFFFFFFFFu, jj);
-    const unsigned long long mkey = ((unsigned long long)mhi << 32) | mlo;
-    if (lane == s + u - s0 && mkey < best) {  // later rounds hold larger indices: ties keep the earlier
-      best = mkey;
-      best_j = (int)mj;
-    }
+  // the warp's smallest (rij, j): high word, then low word, then index
+  const unsigned long long key = valid ? (unsigned long long)__double_as_longlong(rij) : ~0ull;
+  const unsigned hi = (unsigned)(key >> 32);
+  const unsigned mhi = __reduce_min_sync(0xFFFFFFFFu, hi);
+  const unsigned lo = (hi == mhi) ? (unsigned)key : 0xFFFFFFFFu;
+  const unsigned mlo = __reduce_min_sync(0xFFFFFFFFu, lo);
+  const unsigned jj = (hi == mhi && (unsigned)key == mlo) ? (unsigned)j : 0xFFFFFFFFu;
+  const unsigned mj = __reduce_min_sync(0xFFFFFFFFu, jj);
+  const unsigned long long mkey = ((unsigned long long)mhi << 32) | mlo;
+  if (lane == s - s0 && mkey < best) {  // later rounds hold larger indices: ties keep the earlier
+    best = mkey;
+    best_j = (int)mj;
   }
 }
 
-__global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx fc, const double* __restrict__ y,
+__global__ void __launch_bounds__(kWideWarps * 32, kWideCtasPerSm) k_gravity_ac_wide(ForceCtx fc, const double* __restrict__ y,
                                                                         double* __restrict__ dydt, TimeSpec ts,
                                                                         uint32_t flags, int spc) {
   extern __shared__ __align__(16) double wide_terms[];  // [kWideTile][kWideRow]
@@ -613,8 +603,8 @@ __global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx
   const double* src = fc.src;
   const int np = fc.npad;
 
-  // lane s of every warp: the first minimum of sink h ceil(spc/2) + s
-  // (h = warp / 4) over this warp's sources
+  // lane s of every warp: the first minimum of sink g ceil(spc/4) + s
+  // (g = warp / 2, its quarter of the sinks) over this warp's sources
   unsigned long long best = (unsigned long long)__double_as_longlong(1.0e10);
   int best_j = -1;
   // phase-B lanes: component warp, sink lane
@@ -626,9 +616,9 @@ __global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx
     // ---- phase A ----
     {
       const int p = threadIdx.x % kWideTile;
-      const int half = (spc + 1) >> 1;
-      const int s0 = (threadIdx.x / kWideTile) * half;
-      const int s1 = min(s0 + half, spc);
+      const int quarter = (spc + kWideGroups - 1) / kWideGroups;
+      const int s0 = (threadIdx.x / kWideTile) * quarter;
+      const int s1 = min(s0 + quarter, spc);
       const int j = r * kWideTile + p;
       const bool jin = j < ns_cta;
       double xj = 0, yj = 0, zj = 0, gm = 0, px = 0, py = 0, pz = 0;
@@ -642,14 +632,8 @@ __global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx
         pz = src[SPZ * np + j];
       }
       double* row = wide_terms + (size_t)p * kWideRow;
-      // two sinks per step, branch-free up to the stores, so that their
-      // dependency chains interleave; an odd last sink takes a step alone
-      for (int s = s0; s < s1; s += 2) {
-        if (s + 1 < s1)
-          wide_sinks<2>(s, s0, j, jin, i0, lane, xj, yj, zj, gm, px, py, pz, sink_pos, sink_ns, row, best, best_j);
-        else
-          wide_sinks<1>(s, s0, j, jin, i0, lane, xj, yj, zj, gm, px, py, pz, sink_pos, sink_ns, row, best, best_j);
-      }
+      for (int s = s0; s < s1; ++s)
+        wide_sink(s, s0, j, jin, i0, lane, xj, yj, zj, gm, px, py, pz, sink_pos, sink_ns, row, best, best_j);
     }
     __syncthreads();
     // ---- phase B ----
@@ -679,12 +663,13 @@ __global__ void __launch_bounds__(kWideWarps * 32, 2) k_gravity_ac_wide(ForceCtx
     fc.nn_dist[0] = 0.0;
     return;
   }
-  const int half = (spc + 1) >> 1;
-  const int w0 = (s / half) * (kWideWarps / 2);
-  const int hl = s % half;
+  constexpr int kWarpsPerGroup = kWideTile / 32;
+  const int quarter = (spc + kWideGroups - 1) / kWideGroups;
+  const int w0 = (s / quarter) * kWarpsPerGroup;
+  const int hl = s % quarter;
   unsigned long long bk = nn_key[w0][hl];
   int bj = nn_j[w0][hl];
-  for (int w = w0 + 1; w < w0 + kWideWarps / 2; ++w) {
+  for (int w = w0 + 1; w < w0 + kWarpsPerGroup; ++w) {
     const unsigned long long k2 = nn_key[w][hl];
     const int j2 = nn_j[w][hl];
     if (j2 >= 0 && (bj < 0 || k2 < bk || (k2 == bk && j2 < bj))) {
@@ -1164,7 +1149,7 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
     }
     // sinks per CTA: the fewest whole waves of two CTAs per SM, then the
     // cheapest of that and the next two wave counts
-    const int slots = 2 * wide_sms[dev];
+    const int slots = kWideCtasPerSm * wide_sms[dev];
     int spc = 0;
     {
       const int k0 = (c->n + slots * kWideSinks - 1) / (slots * kWideSinks);
