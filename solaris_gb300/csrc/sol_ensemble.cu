@@ -274,13 +274,13 @@ __global__ void k_ensemble_rkf78(const EnsSys* __restrict__ systems, const int* 
           if (em < 1.0) {
             C.h_did = h;
             C.t += C.h_did;
-            C.h_next = em > 1.89e-4 ? (0.9 * h * pow(em, -0.2)) : (5.0 * h);
+            C.h_next = em > 1.89e-4 ? (0.9 * h * sol_inv_root<5>(em)) : (5.0 * h);
             C.h = C.h_next;
             C.accepted = 1;
             C.n_acc++;
           } else {
             C.n_rej++;
-            double hTemp = 0.9 * h * pow(em, -0.25);
+            double hTemp = 0.9 * h * sol_inv_root<4>(em);
             double hn = fabs(hTemp) > fabs(0.1 * h) ? hTemp : 0.1 * h;
             C.h = hn;
             if (C.t + hn == C.t) C.status = SOL_ERR_UNDERFLOW;

@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
         if (em < 1.0) {
           S.h_did = h;
           S.t += S.h_did;
-          S.h_next = em > 1.89e-4 ? (0.9 * h * pow(em, -0.2)) : (5.0 * h);
+          S.h_next = em > 1.89e-4 ? (0.9 * h * sol_inv_root<5>(em)) : (5.0 * h);
           S.h = S.h_next;
           S.accepted = 1;
           S.n_acc++;
@@ -699,7 +699,7 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
           }
         } else {
           S.n_rej++;
-          const double hTemp = 0.9 * h * pow(em, -0.25);
+          const double hTemp = 0.9 * h * sol_inv_root<4>(em);
           const double hn = fabs(hTemp) > fabs(0.1 * h) ? hTemp : 0.1 * h;
           S.h = hn;
           if (S.t + hn == S.t) S.status |= SOL_DEV_UNDERFLOW;

@@ -131,13 +131,13 @@ __global__ void k_control_rkf78(sol_ctrl* c, cudaGraphConditionalHandle hcond, i
   if (em < 1.0) {
     c->h_did = h;
     c->t += c->h_did;
-    c->h_next = em > 1.89e-4 ? (0.9 * h * pow(em, -0.2)) : (5.0 * h);
+    c->h_next = em > 1.89e-4 ? (0.9 * h * sol_inv_root<5>(em)) : (5.0 * h);
     c->h = c->h_next;
     c->accepted = 1;
     c->n_accepted++;
   } else {
     c->n_rejected++;
-    double hTemp = 0.9 * h * pow(em, -0.25);
+    double hTemp = 0.9 * h * sol_inv_root<4>(em);
     double hn = fabs(hTemp) > fabs(0.1 * h) ? hTemp : 0.1 * h;
     c->h = hn;
     double tNew = c->t + hn;

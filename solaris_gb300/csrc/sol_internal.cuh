@@ -252,6 +252,52 @@ __device__ __forceinline__ bool sol_mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+// ---- step-size control powers ------------------------------------------------
+// em^(-1/N) for the RKF78 control's pow(errorMax, PGROW = -0.2) and
+// pow(errorMax, PSHRNK = -0.25) (RungeKuttaFehlberg78.cpp:61-62, :113, :129),
+// correctly rounded but for values within ~2^-100 relative of a midpoint, as
+// the reference's libm pow is in practice (a retried step's h differing in
+// the last bit moves the next error estimate far more, through its
+// cancellation).  A library pow is a chain of ~5,800 cycles on the GPU, on
+// the critical path of every attempt of the latency-bound drivers.  Here:
+// an FP32 seed exp2(-log2(em)/N) (relative error < 2^-17 for |log2 em| <=
+// 100), two Newton steps for em y^N = 1, y <- y + (y/N)(1 - em y^N)
+// (2^-17 -> 2^-33 -> 2^-64 plus rounding), then the residual 1 - em y^N in
+// double-double (TwoProduct by FMA; 1 - q is exact by Sterbenz) and one
+// correction y + y t / N added with a single rounding.  Outside
+// 2^-100 < em < 2^100 the library pow is taken.
+template <int N>
+__device__ __forceinline__ double sol_inv_root(double em) {
+  const unsigned hi = (unsigned)__double2hiint(em);
+  const int e = (int)(hi >> 20) - 1023;  // em > 0
+  if (e <= -100 || e >= 100) return pow(em, -1.0 / N);
+  const float ef = __uint_as_float(((unsigned)(e + 127) << 23) | ((hi & 0xFFFFFu) << 3));
+  const float ys = exp2f(-__log2f(ef) * (1.0f / N));
+  const unsigned yb = __float_as_uint(ys);
+  double y = __hiloint2double((int)((((yb >> 23) - 127 + 1023) << 20) | ((yb & 0x7FFFFFu) >> 3)), (int)(yb << 29));
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const double y2 = y * y;
+    const double yn = (N == 4) ? y2 * y2 : (y2 * y2) * y;
+    const double t = __fma_rn(-em, yn, 1.0);
+    y = __fma_rn(y * (1.0 / N), t, y);
+  }
+  // y^N as p + pe (double-double), then em y^N as q + qe
+  const double p2 = y * y;
+  const double e2 = __fma_rn(y, y, -p2);
+  const double p4 = p2 * p2;
+  const double e4 = __fma_rn(p2, p2, -p4) + 2.0 * p2 * e2;
+  double p = p4, pe = e4;
+  if (N == 5) {
+    p = p4 * y;
+    pe = __fma_rn(p4, y, -p) + e4 * y;
+  }
+  const double q = em * p;
+  const double qe = __fma_rn(em, p, -q) + em * pe;
+  const double t = (1.0 - q) - qe;
+  return y + y * t * (1.0 / N);
+}
+
 // ---- gas-model device functions (restated from Solaris/GasComponent.cpp) ----
 __device__ __forceinline__ double sol_pl(double c, double idx, double x) { return c * pow(x, idx); }
 

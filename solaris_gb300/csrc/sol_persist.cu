@@ -301,13 +301,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_persist_rkf78(PersistArgs P) {
         if (em < 1.0) {
           S.h_did = h;
           S.t += S.h_did;
-          S.h_next = em > 1.89e-4 ? (0.9 * h * pow(em, -0.2)) : (5.0 * h);
+          S.h_next = em > 1.89e-4 ? (0.9 * h * sol_inv_root<5>(em)) : (5.0 * h);
           S.h = S.h_next;
           S.accepted = 1;
           S.n_acc++;
         } else {
           S.n_rej++;
-          const double hTemp = 0.9 * h * pow(em, -0.25);
+          const double hTemp = 0.9 * h * sol_inv_root<4>(em);
           const double hn = fabs(hTemp) > fabs(0.1 * h) ? hTemp : 0.1 * h;
           S.h = hn;
           if (S.t + hn == S.t) S.status |= SOL_DEV_UNDERFLOW;
