@@ -653,12 +653,22 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
       }
       ok = group_barrier(P, &S.abort);
       if (!ok) break;
-      if (threadIdx.x == 0) {  // every CTA takes the same decision (:98-133)
-        double mx = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) {
+      // warp 0 gathers every CTA's partial maximum and event flag at once
+      double mx = 0.0;
+      int any_ev = 0;
+      if (threadIdx.x < 32) {
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
           const double o = gridDim.x > 1 ? __ldcg(partial + b) : V.red[0];
-          if (o > mx) mx = o;
+          mx = o > mx ? o : mx;
+          if (P.sim) any_ev |= gridDim.x > 1 ? __ldcg(evp + b) : S.event;
         }
+        for (int w = 16; w > 0; w >>= 1) {
+          const double o = __shfl_xor_sync(0xFFFFFFFFu, mx, w);
+          mx = o > mx ? o : mx;
+        }
+        any_ev = (int)__reduce_or_sync(0xFFFFFFFFu, (unsigned)any_ev);
+      }
+      if (threadIdx.x == 0) {  // every CTA takes the same decision (:98-133)
         const double em = mx / S.eps;
         S.error_max = em;
         if (em < 1.0) {
@@ -669,8 +679,7 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
           S.accepted = 1;
           S.n_acc++;
           if (P.sim) {  // Simulator::DecisionMaking up to where the host has work (Simulator.cpp:181-250)
-            int any = 0;
-            for (int b = 0; b < (int)gridDim.x; ++b) any |= gridDim.x > 1 ? __ldcg(evp + b) : S.event;
+            const int any = any_ev;
             sol_sim_line& L = S.L;
             L.steps += 1;
             L.elapsed += S.h_did;
