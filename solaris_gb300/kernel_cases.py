@@ -3,7 +3,7 @@
     python -m solaris_gb300.kernel_cases <case>
 
 Cases (each sized to a few hundred MB of device memory at most):
-  fp64_few       k_gravity_ac_few: FP64 force, 4,096 self-gravitating bodies
+  fp64_few       k_gravity_ac_few: FP64 force, 2,048 self-gravitating bodies
   fp64_wide      k_gravity_ac_wide: FP64 force, 16,384 self-gravitating bodies
   split_ff_warp  k_pairs_few<SPLIT_FF>: float-float force, 4,096 bodies
   split_ff_2d    k_pairs<SPLIT_FF> + k_combine: float-float force, 32,768 bodies
@@ -26,7 +26,7 @@ from solaris_gb300 import abi, engine, scenarios
 
 def run(case: str) -> None:
     if case in ("fp64_few", "fp64_wide", "split_ff_warp", "split_ff_2d"):
-        n = {"split_ff_2d": 32768, "fp64_wide": 16384}.get(case, 4096)
+        n = {"split_ff_2d": 32768, "fp64_wide": 16384, "fp64_few": 2048}.get(case, 4096)
         prec = abi.PRECISION_FP64 if case.startswith("fp64") else abi.PRECISION_SPLIT_FF
         s = scenarios.config3(n=n)
         with engine.Context(s, precision=prec) as ctx:
