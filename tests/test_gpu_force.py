@@ -211,3 +211,27 @@ def test_split_ff_close_pairs_and_coincident_sink(n):
     assert np.isfinite(dff).all()
     assert rel_accel_err(dff, ref).max() <= SPLIT_RTOL
     assert nn[10] == 9 and nn[9] == 10 and nn[20] == 19
+
+
+@pytest.mark.parametrize("n", [400, 4000])
+def test_fp64_fallback_paths_bit_identical(n):
+    """The FP64 kernels' rare fallbacks against the oracle, bit for bit: two
+    bodies 1e-93 and 2e-93 AU from the star (their rm3 and their pair have
+    squared distances below 2^-600: IEEE sqrt and division instead of the
+    FMA-remainder rounding) and a source of subnormal mass (its term
+    multiplies leave the integer pipe for the FP64 instruction).  400 bodies
+    run the 4-sink kernel, 4,000 the 32-sink kernel."""
+    s = scenarios.config3(seed=7000 + n, n=n)
+    y = s.y0.reshape(-1, 6)
+    y[5, :3] = (1.0e-93, 0.0, 0.0)
+    y[7, :3] = (2.0e-93, 0.0, 0.0)
+    s.mass[9] = 1.0e-310
+    o = oracle.Oracle(s)
+    ref = o.compute(0.0, s.y0)
+    rm3_o, nn_o, nd_o = o.last_eval()
+    with engine.Context(s) as ctx:
+        d64, rm3, nn, nd = ctx.accel(0.0, s.y0)
+    assert np.array_equal(bits(d64), bits(ref))
+    assert np.array_equal(bits(rm3), bits(rm3_o))
+    assert np.array_equal(nn, nn_o) and np.array_equal(bits(nd), bits(nd_o))
+    assert nn[5] == 7 and nn[7] == 5
