@@ -30,10 +30,11 @@
 // midpoint needs 54 significant bits; its square, or its product with a
 // 53-bit d, cannot be a double, resp. 1).  Where the measured distance lies
 // within 2^-16 ulp of a midpoint (probability ~2^-15 per function), where
-// the result would land on or cross a power of two, or where a is outside
-// [2^-600, 2^600] (zero, denormal, infinite or NaN included) the fast path
-// reports failure and the caller takes IEEE sqrt and division, so the result
-// is the correctly rounded one in every case.
+// it exceeds 2^20 ulp (an approximation gone astray), where the result would
+// land on or cross a power of two, or where a is outside [2^-600, 2^600]
+// (zero, denormal, infinite or NaN included) the fast path reports failure
+// and the caller takes IEEE sqrt and division, so the result is the
+// correctly rounded one in every case.
 #pragma once
 
 #include "sol_pair.cuh"
