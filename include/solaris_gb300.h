@@ -480,7 +480,10 @@ int sol_measure_fp64_peak(int32_t device, double* flops);
  * ulps off; 4: log-uniform reciprocals from such approximations; 5: square
  * roots and reciprocals next to powers of two; 6: the integer-pipe double
  * multiply of the pair terms against the FP64 instruction, random operands;
- * 7: the same next to the normalisation boundaries, zeros and squares).
+ * 7: the same next to the normalisation boundaries, zeros and squares;
+ * 8, 9: the RKF78 step-size control's errorMax^-1/5 and errorMax^-1/4,
+ * checked for correct rounding by the sign of em t^N - 1 at the midpoints
+ * around each result).
  * result[0] = samples whose fast path disagrees (0 when correct),
  * result[1] = samples the fast path hands to IEEE sqrt and division,
  * result[2] = the first disagreeing sample's index, or -1. */

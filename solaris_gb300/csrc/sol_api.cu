@@ -895,7 +895,7 @@ int sol_measure_fp64_peak(int32_t device, double* flops) {
 }
 
 int sol_check_pair_math(int32_t device, int32_t mode, int64_t n, uint64_t seed, int64_t result[3]) {
-  if (!result || mode < 0 || mode > 7 || n < 0) return SOL_ERR_ARG;
+  if (!result || mode < 0 || mode > 9 || n < 0) return SOL_ERR_ARG;
   long long r[3];
   RET(sol_check_pair_math_launch(device, mode, (long long)n, (unsigned long long)seed, r));
   for (int k = 0; k < 3; ++k) result[k] = r[k];

@@ -107,7 +107,11 @@ __global__ void k_dfma_peak(double seed, double b, double* out, int iters) {
 //   6: the integer-pipe multiply sol_exact_dmul against the FP64 instruction,
 //      random signed operands with exponents over [2^-300, 2^300];
 //   7: the same with significands whose product sits next to 2^104 or 2^106,
-//      zeros and squares.
+//      zeros and squares;
+//   8, 9: the step-size roots em^-1/5 and em^-1/4 (sol_inv_root), em
+//      log-uniform over [2^-13, 2^30]: correctly rounded iff em t^N - 1,
+//      evaluated in double-double at the midpoints t = y -+ ulp/2, changes
+//      sign between them.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
   x += 0x9E3779B97F4A7C15ull;
   x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -117,6 +121,23 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
 
 __device__ __forceinline__ double unit_double(unsigned long long h) { return (double)(h >> 11) * 0x1.0p-53; }
 
+
+// em t^N - 1 for t = th + tl (double-double), in double-double; its sign
+__device__ __forceinline__ int root_residual_sign(double em, double th, double tl, int N) {
+  // p = t^N by repeated double-double multiplication
+  double ph = th, pl = tl;
+  for (int k = 1; k < N; ++k) {
+    const double h = ph * th;
+    const double l = __fma_rn(ph, th, -h) + (ph * tl + pl * th);
+    ph = h + l;
+    pl = l - (ph - h);
+  }
+  const double qh = em * ph;
+  const double ql = __fma_rn(em, ph, -qh) + em * pl;
+  const double d = (qh - 1.0) + ql;  // qh - 1 is exact (qh near 1)
+  return (d > 0.0) - (d < 0.0);
+}
+
 __global__ void k_check_rinv3(int mode, long long n, unsigned long long seed, unsigned long long* counts,
                               long long* first) {
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -124,7 +145,16 @@ __global__ void k_check_rinv3(int mode, long long n, unsigned long long seed, un
     const unsigned long long h1 = mix64(seed ^ mix64((unsigned long long)s));
     const unsigned long long h2 = mix64(h1);
     bool ok = true, bad = false;
-    if (mode >= 6) {
+    if (mode >= 8) {
+      const long long E = 1023 - 13 + (long long)(h2 % 44);
+      const double em = __longlong_as_double((E << 52) | (long long)(h1 & 0xFFFFFFFFFFFFFull));
+      const int N = mode == 8 ? 5 : 4;
+      const double y = N == 5 ? sol_inv_root<5>(em) : sol_inv_root<4>(em);
+      const long long yb = __double_as_longlong(y);
+      const double half = 0.5 * (__longlong_as_double(yb + 1) - y);   // half an ulp above y
+      const double halfd = 0.5 * (y - __longlong_as_double(yb - 1));  // half an ulp below y
+      bad = !(root_residual_sign(em, y, -halfd, N) <= 0 && root_residual_sign(em, y, half, N) >= 0);
+    } else if (mode >= 6) {
       unsigned long long ea = 1023 - 300 + (h1 >> 52) % 601, eb = 1023 - 300 + (h2 >> 52) % 601;
       unsigned long long ma = h1 & 0xFFFFFFFFFFFFFull, mb = h2 & 0xFFFFFFFFFFFFFull;
       if (mode == 7) {

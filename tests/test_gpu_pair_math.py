@@ -2,7 +2,8 @@
 (sol_crmath.cuh: remainders by FMA, rounding decided from the measured
 distance to the neighbouring doubles) against IEEE sqrt and division, and
 the integer-pipe multiply of the pair terms against the FP64 instruction,
-bit for bit, on seeded sample families (sol_check_pair_math)."""
+bit for bit, and the step-size control's inverse roots for correct
+rounding, on seeded sample families (sol_check_pair_math)."""
 import pytest
 
 from solaris_gb300 import engine
@@ -21,6 +22,8 @@ N = 1 << 28
     (5, 0.4),    # square roots and reciprocals next to powers of two (results on a power of two go the IEEE way)
     (6, 0.0),    # integer-pipe multiply, random operands
     (7, 0.0),    # integer-pipe multiply next to the normalisation boundaries, zeros, squares
+    (8, 0.0),    # step-size control errorMax^-1/5: correctly rounded
+    (9, 0.0),    # step-size control errorMax^-1/4: correctly rounded
 ])
 def test_pair_math_matches_ieee(mode, max_slow):
     r = engine.check_pair_math(mode, N, seed=1000 + mode)
