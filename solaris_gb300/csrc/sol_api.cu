@@ -790,6 +790,8 @@ int sol_check_events(sol_ctx* c, double ejection, double hit_centrum, double col
   return SOL_OK;
 }
 
+constexpr int kExactPotentialMax = 1024;
+
 int sol_integrals(sol_ctx* c, const double* y0_or_null, double o[16]) {
   RET(check_ctx(c));
   if (!o) return SOL_ERR_ARG;
@@ -801,8 +803,15 @@ int sol_integrals(sol_ctx* c, const double* y0_or_null, double o[16]) {
     SOL_CUDA(cudaMemcpyAsync(c->d_io_in, y0_or_null, sizeof(double) * c->nv, cudaMemcpyHostToDevice, c->stream));
     d_y = c->d_io_in;
   }
-  RET(sol_potential_launch(c, d_y, c->d_io_out));
-  SOL_CUDA(cudaMemcpyAsync(pe.data(), c->d_io_out, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+  // Calculate::PotentialEnergy (Calculate.cpp:139-159) adds every ordered
+  // pair into one running sum.  Up to kExactPotentialMax bodies (scenario
+  // sizes, ~1 M pairs at most) that sum runs here in the reference's order,
+  // bit for bit; above, the device sums per body and the host sums those.
+  const bool exact_order = N <= kExactPotentialMax;
+  if (!exact_order) {
+    RET(sol_potential_launch(c, d_y, c->d_io_out));
+    SOL_CUDA(cudaMemcpyAsync(pe.data(), c->d_io_out, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+  }
   SOL_CUDA(cudaMemcpyAsync(y.data(), d_y, sizeof(double) * c->nv, cudaMemcpyDeviceToHost, c->stream));
   SOL_CUDA(cudaMemcpyAsync(mass.data(), c->d_mass, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
   SOL_CUDA(cudaStreamSynchronize(c->stream));
@@ -836,7 +845,22 @@ int sol_integrals(sol_ctx* c, const double* y0_or_null, double o[16]) {
   }
   o[13] = ke;
   double pes = 0.0;
-  for (int i = 0; i < N; i++) pes += pe[i];
+  if (exact_order) {
+    for (int i = 0; i < N; i++) {
+      const double* pi = &y[6 * i];
+      for (int j = 0; j < N; j++) {
+        if (i == j) continue;
+        const double* pj = &y[6 * j];
+        const double dx = pj[0] - pi[0];
+        const double dy = pj[1] - pi[1];
+        const double dz = pj[2] - pi[2];
+        const double rij = sqrt(dx * dx + dy * dy + dz * dz);
+        pes += mass[i] * mass[j] / rij;
+      }
+    }
+  } else {
+    for (int i = 0; i < N; i++) pes += pe[i];
+  }
   o[14] = pes * (0.5 * 2.959122082855911025e-4);
   o[15] = o[13] - o[14];
   return SOL_OK;

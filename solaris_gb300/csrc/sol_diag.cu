@@ -108,10 +108,12 @@ __global__ void k_dfma_peak(double seed, double b, double* out, int iters) {
 //      random signed operands with exponents over [2^-300, 2^300];
 //   7: the same with significands whose product sits next to 2^104 or 2^106,
 //      zeros and squares;
-//   8, 9: the step-size roots em^-1/5 and em^-1/4 (sol_inv_root), em
-//      log-uniform over [2^-13, 2^30]: correctly rounded iff em t^N - 1,
-//      evaluated in double-double at the midpoints t = y -+ ulp/2, changes
-//      sign between them.
+//   8, 9: the step-size powers pow(em, -0.2) and pow(em, -0.25)
+//      (sol_inv_root; the exponent is the double -0.2, slightly beyond -1/5),
+//      em log-uniform over [2^-13, 2^30]: y = em^-e is correctly rounded iff
+//      em^(N e) t^N - 1 (N e = 1 + 5 delta for the double 0.2), evaluated in
+//      double-double at the midpoints t = y -+ ulp/2, changes sign between
+//      them.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
   x += 0x9E3779B97F4A7C15ull;
   x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -122,8 +124,9 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
 __device__ __forceinline__ double unit_double(unsigned long long h) { return (double)(h >> 11) * 0x1.0p-53; }
 
 
-// em t^N - 1 for t = th + tl (double-double), in double-double; its sign
-__device__ __forceinline__ int root_residual_sign(double em, double th, double tl, int N) {
+// em' t^N - 1 for t = th + tl (double-double), em' = em + el, in
+// double-double; its sign
+__device__ __forceinline__ int root_residual_sign(double em, double el, double th, double tl, int N) {
   // p = t^N by repeated double-double multiplication
   double ph = th, pl = tl;
   for (int k = 1; k < N; ++k) {
@@ -133,7 +136,7 @@ __device__ __forceinline__ int root_residual_sign(double em, double th, double t
     pl = l - (ph - h);
   }
   const double qh = em * ph;
-  const double ql = __fma_rn(em, ph, -qh) + em * pl;
+  const double ql = __fma_rn(em, ph, -qh) + (em * pl + el * ph);
   const double d = (qh - 1.0) + ql;  // qh - 1 is exact (qh near 1)
   return (d > 0.0) - (d < 0.0);
 }
@@ -153,7 +156,9 @@ __global__ void k_check_rinv3(int mode, long long n, unsigned long long seed, un
       const long long yb = __double_as_longlong(y);
       const double half = 0.5 * (__longlong_as_double(yb + 1) - y);   // half an ulp above y
       const double halfd = 0.5 * (y - __longlong_as_double(yb - 1));  // half an ulp below y
-      bad = !(root_residual_sign(em, y, -halfd, N) <= 0 && root_residual_sign(em, y, half, N) >= 0);
+      // em^(N e) = em em^(N delta) = em (1 + N delta ln em)
+      const double el = N == 5 ? em * (5.0 / 90071992547409920.0) * log(em) : 0.0;
+      bad = !(root_residual_sign(em, el, y, -halfd, N) <= 0 && root_residual_sign(em, el, y, half, N) >= 0);
     } else if (mode >= 6) {
       unsigned long long ea = 1023 - 300 + (h1 >> 52) % 601, eb = 1023 - 300 + (h2 >> 52) % 601;
       unsigned long long ma = h1 & 0xFFFFFFFFFFFFFull, mb = h2 & 0xFFFFFFFFFFFFFull;

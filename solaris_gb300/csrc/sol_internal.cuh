@@ -253,12 +253,19 @@ __device__ __forceinline__ bool sol_mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // ---- step-size control powers ------------------------------------------------
-// em^(-1/N) for the RKF78 control's pow(errorMax, PGROW = -0.2) and
+// pow(em, -e) for the RKF78 control's pow(errorMax, PGROW = -0.2) and
 // pow(errorMax, PSHRNK = -0.25) (RungeKuttaFehlberg78.cpp:61-62, :113, :129),
-// correctly rounded but for values within ~2^-100 relative of a midpoint, as
-// the reference's libm pow is in practice (a retried step's h differing in
-// the last bit moves the next error estimate far more, through its
-// cancellation).  A library pow is a chain of ~5,800 cycles on the GPU, on
+// with e the double nearest 1/N, correctly rounded, as the reference's libm
+// pow is but for ~8e-4 of its calls (measured for e = 0.2: it lands on the
+// other neighbour of values within ~4e-4 ulp of a midpoint); a step's h
+// differing in the last bit moves the next error estimate far more, through
+// its cancellation.  The double 0.2
+// exceeds 1/5 by 1/90071992547409920: em^-e = em^(-1/5) (1 - delta ln em),
+// a shift of up to ~0.4 ulp that the final correction carries; ln em comes
+// from FP32 (error ~1e-6), which leaves results within ~1e-7 ulp of a
+// midpoint undecided (measured: 5e-8 of samples round the other way,
+// a band 4,000 times narrower than libm's).  For N = 4 the result is
+// correctly rounded but within ~2^-100 of a midpoint.  A library pow is a chain of ~5,800 cycles on the GPU, on
 // the critical path of every attempt of the latency-bound drivers.  Here:
 // an FP32 seed exp2(-log2(em)/N) (relative error < 2^-17 for |log2 em| <=
 // 100), two Newton steps for em y^N = 1, y <- y + (y/N)(1 - em y^N)
@@ -295,7 +302,46 @@ __device__ __forceinline__ double sol_inv_root(double em) {
   const double q = em * p;
   const double qe = __fma_rn(em, p, -q) + em * pe;
   const double t = (1.0 - q) - qe;
-  return y + y * t * (1.0 / N);
+  // the exponent's own rounding: RN(1/N) - 1/N (0 for N = 4)
+  constexpr double kDelta = (N == 5) ? 1.0 / 90071992547409920.0 : 0.0;
+  const double corr = (N == 5) ? t * (1.0 / N) - kDelta * (double)__logf(ef) : t * (1.0 / N);
+  return y + y * corr;
+}
+
+// pow(x, 1.0 / 7.0) of DormandPrince's step control (DormandPrince.cpp:156),
+// correctly rounded as libm's pow is in practice: the library pow (within a
+// few ulp) is stepped to the neighbour where x' - t^7 changes sign between
+// the midpoints around it, x' = x^(7 e) = x (1 + 7 delta ln x), e the double
+// nearest 1/7, delta = e - 1/7 = -1/126100789566373888, everything in
+// double-double.  One thread per attempt evaluates it: latency is no concern.
+__device__ __forceinline__ int seventh_residual_sign(double xh, double xl, double th, double tl) {
+  double ph = th, pl = tl;
+  for (int k = 1; k < 7; ++k) {
+    const double h = ph * th;
+    const double l = __fma_rn(ph, th, -h) + (ph * tl + pl * th);
+    ph = h + l;
+    pl = l - (ph - h);
+  }
+  const double d = (ph - xh) + (pl - xl);  // ph - xh is exact: t^7 and x agree to a few ulp
+  return (d > 0.0) - (d < 0.0);
+}
+
+static __device__ __noinline__ double sol_pow_one_seventh(double x) {
+  double y = pow(x, 1.0 / 7.0);
+  if (!(x > 0.0) || !(y > 0.0) || !(y < 1.0e300)) return y;
+  const double xl = x * (7.0 * (-1.0 / 126100789566373888.0)) * log(x);
+  for (int it = 0; it < 4; ++it) {
+    const long long yb = __double_as_longlong(y);
+    const double up = 0.5 * (__longlong_as_double(yb + 1) - y);
+    const double dn = 0.5 * (y - __longlong_as_double(yb - 1));
+    if (seventh_residual_sign(x, xl, y, -dn) > 0)
+      y = __longlong_as_double(yb - 1);  // the root lies below the lower midpoint
+    else if (seventh_residual_sign(x, xl, y, up) < 0)
+      y = __longlong_as_double(yb + 1);
+    else
+      break;
+  }
+  return y;
 }
 
 // ---- gas-model device functions (restated from Solaris/GasComponent.cpp) ----

@@ -2,9 +2,12 @@
 
 With the FP64 force the stage sums, final sums and error estimates follow
 the reference's operation order and are bit-identical per attempt.  The step
-controls call pow(), whose last bit may differ between CUDA and glibc, so
-multi-step trajectories of the adaptive methods are compared to a tolerance;
-RungeKutta4 has no pow and stays bit-identical over many steps."""
+controls' powers (pow(errorMax, -0.2 / -0.25), pow(eps / errorMax, 1/7)) are
+correctly rounded on the device; libm's pow is too but for ~8e-4 of its
+calls, so driver calls agree bit for bit and long adaptive runs until the
+reference's pow first misrounds.  Gas drag and migration use CUDA's pow /
+exp / log10, whose last bit may differ from glibc: those systems are
+compared to a tolerance."""
 import numpy as np
 import pytest
 
@@ -92,17 +95,10 @@ def _per_step(system, integrator, n_steps, h0, exact):
             r = ctx.driver(integrator, 0, 0, 1, time_line=tl)
             yg = ctx.get_state()
             assert r["stats"][:2] == ro["stats"][:2], f"step {k}: accepted/rejected differ"
-            # After a rejected attempt the retry uses h = 0.9 h errorMax^-1/4, and
-            # pow() may round differently in the last bit on the GPU: such steps
-            # are compared to rounding level, the others bit for bit.
-            if exact and r["stats"][1] == 0:
+            if exact:  # accepted, rejected and retried attempts alike
                 assert np.array_equal(bits(yg), bits(ro["y0"])), f"step {k}"
-                assert tl.time == ro["tl"][0] and tl.h_did == ro["tl"][2]
-                assert abs(tl.h_next - ro["tl"][1]) <= 4e-16 * abs(ro["tl"][1])
-            elif exact:
-                assert body_rel(yg, ro["y0"]).max() <= 1e-13, f"step {k}"
-                assert abs(tl.h_did - ro["tl"][2]) <= 4e-16 * abs(ro["tl"][2])
-                assert abs(tl.h_next - ro["tl"][1]) <= 1e-15 * abs(ro["tl"][1])
+                assert tl.time == ro["tl"][0] and tl.h_did == ro["tl"][2], f"step {k}"
+                assert tl.h_next == ro["tl"][1], f"step {k}"
             else:
                 # with gas drag the error norm carries pow/exp rounding amplified
                 # by the cancellation in the error estimate: a retried step's h
@@ -132,10 +128,14 @@ def test_dormand_prince_driver_per_step_config1():
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_SPLIT])
 def test_rkf78_long_run_statistics(precision):
     """500 device-driven RKF78 steps (device-side accept/reject).  Adaptive
-    control is chaotic at the last bit (pow rounding), so the comparison with
-    the oracle is statistical: step counts and reached time agree to a few
-    per cent.  (The heliocentric energy of Calculate::Integrals is not a
-    conserved quantity, the frame being non-inertial.)"""
+    control is chaotic at the last bit and libm's pow, which the oracle and
+    the reference call, is not quite correctly rounded (measured: 8e-4 of
+    pow(errorMax, -0.2) calls land on the other neighbour of a near-midpoint
+    value), so over ~800 calls the device's correctly rounded power parts
+    from it once or so: the comparison is statistical, step counts and
+    reached time agree to a few per cent.  (The heliocentric energy of
+    Calculate::Integrals is not a conserved quantity, the frame being
+    non-inertial.)"""
     s = scenarios.config1(seed=1501)
     o = oracle.Oracle(s)
     ref = o.driver(abi.RUNGE_KUTTA_FEHLBERG78, s.y0, 0.0, s.h0, 500)
