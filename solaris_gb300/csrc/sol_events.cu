@@ -102,11 +102,11 @@ __device__ void merge(const EvArgs& A, int s, int m) {
   if (A.radius[s] != 0.0) {
     if (A.radius[m] == 0.0) {
       A.density[m] = A.density[s];
-      A.radius[m] = pow(3.0 / (4.0 * SOL_PI) * A.mass[m] / A.density[m], 1.0 / 3.0);
+      A.radius[m] = sol_pow_recip_cr<3>(3.0 / (4.0 * SOL_PI) * A.mass[m] / A.density[m]);
     }
     const double rs = A.radius[s], rm = A.radius[m];
     const double vol = 4.0 / 3.0 * SOL_PI * (rs * rs * rs + rm * rm * rm);
-    A.radius[s] = pow(3.0 / (4.0 * SOL_PI) * vol, 1.0 / 3.0);
+    A.radius[s] = sol_pow_recip_cr<3>(3.0 / (4.0 * SOL_PI) * vol);
     A.density[s] = M / vol;
   }
 }

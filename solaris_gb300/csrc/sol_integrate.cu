@@ -235,7 +235,7 @@ __global__ void k_control_dp(sol_ctrl* c, cudaGraphConditionalHandle hcond, int 
   const double h = c->h;
   c->iter++;
   c->h_did = h;
-  c->h_next = em < 1.0e-20 ? 2.0 * h : 0.9 * h * sol_pow_one_seventh(c->eps / em);
+  c->h_next = em < 1.0e-20 ? 2.0 * h : 0.9 * h * sol_pow_recip_cr<7>(c->eps / em);
   if (em > c->eps && c->iter <= 10) {
     c->n_rejected++;
     c->h = c->h_next;  // the next attempt uses timeLine->hNext

@@ -308,35 +308,40 @@ __device__ __forceinline__ double sol_inv_root(double em) {
   return y + y * corr;
 }
 
-// pow(x, 1.0 / 7.0) of DormandPrince's step control (DormandPrince.cpp:156),
-// correctly rounded as libm's pow is in practice: the library pow (within a
-// few ulp) is stepped to the neighbour where x' - t^7 changes sign between
-// the midpoints around it, x' = x^(7 e) = x (1 + 7 delta ln x), e the double
-// nearest 1/7, delta = e - 1/7 = -1/126100789566373888, everything in
-// double-double.  One thread per attempt evaluates it: latency is no concern.
-__device__ __forceinline__ int seventh_residual_sign(double xh, double xl, double th, double tl) {
+// pow(x, 1.0 / N) for N = 7 (DormandPrince's step control,
+// DormandPrince.cpp:156) and N = 3 (the radius after a merge), correctly
+// rounded: the library pow (within a few ulp) is stepped to the neighbour
+// where x' - t^N changes sign between the midpoints around it,
+// x' = x^(N e) = x (1 + N delta ln x), e the double nearest 1/N and
+// delta = e - 1/N (-1/54043195528445952 for N = 3, -1/126100789566373888 for
+// N = 7), everything in double-double.  One thread evaluates it per attempt
+// or per merge: latency is no concern.
+__device__ __forceinline__ int root_power_sign(double xh, double xl, double th, double tl, int n) {
   double ph = th, pl = tl;
-  for (int k = 1; k < 7; ++k) {
+  for (int k = 1; k < n; ++k) {
     const double h = ph * th;
     const double l = __fma_rn(ph, th, -h) + (ph * tl + pl * th);
     ph = h + l;
     pl = l - (ph - h);
   }
-  const double d = (ph - xh) + (pl - xl);  // ph - xh is exact: t^7 and x agree to a few ulp
+  const double d = (ph - xh) + (pl - xl);  // ph - xh is exact: t^N and x agree to a few ulp
   return (d > 0.0) - (d < 0.0);
 }
 
-static __device__ __noinline__ double sol_pow_one_seventh(double x) {
-  double y = pow(x, 1.0 / 7.0);
+template <int N>
+__device__ __noinline__ double sol_pow_recip_cr(double x) {
+  static_assert(N == 3 || N == 7, "exponent offsets are tabulated for 1/3 and 1/7");
+  constexpr double kDelta = N == 3 ? -1.0 / 54043195528445952.0 : -1.0 / 126100789566373888.0;
+  double y = pow(x, 1.0 / N);
   if (!(x > 0.0) || !(y > 0.0) || !(y < 1.0e300)) return y;
-  const double xl = x * (7.0 * (-1.0 / 126100789566373888.0)) * log(x);
+  const double xl = x * (N * kDelta) * log(x);
   for (int it = 0; it < 4; ++it) {
     const long long yb = __double_as_longlong(y);
     const double up = 0.5 * (__longlong_as_double(yb + 1) - y);
     const double dn = 0.5 * (y - __longlong_as_double(yb - 1));
-    if (seventh_residual_sign(x, xl, y, -dn) > 0)
+    if (root_power_sign(x, xl, y, -dn, N) > 0)
       y = __longlong_as_double(yb - 1);  // the root lies below the lower midpoint
-    else if (seventh_residual_sign(x, xl, y, up) < 0)
+    else if (root_power_sign(x, xl, y, up, N) < 0)
       y = __longlong_as_double(yb + 1);
     else
       break;
