@@ -295,7 +295,12 @@ int sol_get_side_buffers(sol_ctx* ctx, double* drag, double* mig1, double* mig2)
 int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double collision_factor,
                      sol_event* out, int32_t capacity, int32_t* n_out);
 
-/* ---- diagnostics: Calculate::Integrals (Solaris/Calculate.cpp:43-62). --- */
+/* ---- diagnostics: Calculate::Integrals (Solaris/Calculate.cpp:43-62). ---
+ * The 16 values of the reference's integrals record for the context's state
+ * (or y0_or_null).  Up to 1,024 bodies the potential energy is the
+ * reference's single running sum over ordered pairs, bit for bit (on the
+ * host); above, the device sums per body and the host sums those, which may
+ * differ in the last bits. */
 int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
 
 /* ---- output files: BinaryFileAdapter (Solaris/BinaryFileAdapter.cpp:107-219)
