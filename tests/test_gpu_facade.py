@@ -66,9 +66,9 @@ def test_rk4_driver_matches_the_oracle_bit_for_bit(exe, tmp_path):
 
 @pytest.mark.parametrize("integrator", [abi.RUNGE_KUTTA_FEHLBERG78, abi.DORMAND_PRINCE])
 def test_adaptive_driver_matches_the_engine(exe, tmp_path, integrator):
-    """The facade's Driver calls are the engine's driver calls: the same bits
-    step after step (both run on this GPU), and the first step equals the
-    oracle's."""
+    """The facade's Driver calls are the engine's driver calls and the
+    oracle's: the same bits step after step, retried attempts included (the
+    step controls' powers are correctly rounded on the device)."""
     s = scenarios.config1(n_tp=61)
     h0 = s.h0 * (50 if integrator == abi.DORMAND_PRINCE else 1)
     n = 15
@@ -84,10 +84,9 @@ def test_adaptive_driver_matches_the_engine(exe, tmp_path, integrator):
         y = ctx.get_state()
     assert np.array_equal(bits(out["drv_y0"]), bits(y))
     assert np.array_equal(bits(out["drv_time"]), bits(times))
-    one = run(exe, str(tmp_path), s, integrator, 1, 0.0, h0)
-    ro = oracle.Oracle(s).driver(integrator, s.y0, 0.0, h0, 1)
-    if ro["stats"][1] == 0:  # no retry: no pow() in the step taken
-        assert np.array_equal(bits(one["drv_y0"]), bits(ro["y0"]))
+    ro = oracle.Oracle(s).driver(integrator, s.y0, 0.0, h0, n)
+    assert np.array_equal(bits(out["drv_y0"]), bits(ro["y0"]))
+    assert out["drv_time"][-1] == ro["tl"][0]
 
 
 def test_body_removal_between_driver_calls(exe, tmp_path):
