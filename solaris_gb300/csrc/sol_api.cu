@@ -667,8 +667,9 @@ int sol_run_until(sol_ctx* c, int32_t integrator, sol_sim_line* L, int32_t max_s
   RET(ensure_sim(c));
   const double e3 = ejection > 0 ? 1.0 / (ejection * ejection * ejection) : 0.0;
   const double h3 = hit_centrum > 0 ? 1.0 / (hit_centrum * hit_centrum * hit_centrum) : 0.0;
-  // the whole loop on the device: RKF78 systems of few sources
-  if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78 && c->device_loop && sol_group_eligible(c)) {
+  // the whole loop on the device: RKF78 and RK4 systems of few sources
+  const bool rk4 = integrator == SOL_RUNGE_KUTTA4;
+  if ((integrator == SOL_RUNGE_KUTTA_FEHLBERG78 || rk4) && c->device_loop && sol_group_eligible(c)) {
     char* base = static_cast<char*>(c->d_sim);
     GroupSim sim;
     sim.e3 = e3;
@@ -689,7 +690,7 @@ int sol_run_until(sol_ctx* c, int32_t integrator, sol_sim_line* L, int32_t max_s
     SOL_CUDA(cudaMemcpyAsync(c->d_ctrl, &h0, sizeof(h0), cudaMemcpyHostToDevice, c->stream));
     SOL_CUDA(cudaMemcpyAsync(sim.line, L, sizeof(*L), cudaMemcpyHostToDevice, c->stream));
     SOL_CUDA(cudaMemcpyAsync(sim.reason, &stop_steps, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    const int r = sol_group_rkf78(c, max_steps, &sim);
+    const int r = sol_group_rkf78(c, max_steps, &sim, rk4);
     if (r != SOL_ERR_STATE) {
       if (r != SOL_OK) return r;
       SOL_CUDA(cudaMemcpyAsync(c->h_ctrl, c->d_ctrl, sizeof(sol_ctrl), cudaMemcpyDeviceToHost, c->stream));
@@ -701,7 +702,7 @@ int sol_run_until(sol_ctx* c, int32_t integrator, sol_sim_line* L, int32_t max_s
       if (stats) {
         stats->accepted += hc.n_accepted;
         stats->rejected += hc.n_rejected;
-        stats->evaluations += hc.n_accepted * 13 + hc.n_rejected * 12;
+        stats->evaluations += rk4 ? hc.n_accepted * 4 : hc.n_accepted * 13 + hc.n_rejected * 12;
       }
       if (hc.dev_status & SOL_DEV_TIMEOUT) {
         sol_set_error("a bounded device wait ran out");

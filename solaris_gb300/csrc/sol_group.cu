@@ -75,6 +75,7 @@ struct GroupArgs {
   int ns;               // sources: nm + n_spl
   int local;            // other bodies per CTA
   int n_steps;
+  int rk4;              // RungeKutta4 driver calls instead of RungeKuttaFehlberg78
   int sim;              // the Simulator's step loop (sol_run_until)
   double e3, h3, cf;    // its event thresholds (0: off)
   sol_sim_line* line;
@@ -118,6 +119,7 @@ __device__ bool group_barrier(const GroupArgs& P, int* s_abort) {
 }
 
 struct Ctl {
+  double fac[4];  // RungeKutta4: ReductionFactor at the stage times t + c h
   double t, h, h_next, h_did, error_max, eps;
   long long n_acc, n_rej;
   int status, accepted, abort, npair, ndrag, nmig;
@@ -432,7 +434,7 @@ __device__ __noinline__ void evaluate(const GroupArgs& P, const View& V, double 
       }
       fc.nn_idx[i] = nn;
       fc.nn_dist[i] = nn >= 0 ? __longlong_as_double(rminb) : 0.0;
-      if (P.sim && r == 12) {  // CheckEvent's predicates on the attempt's last evaluation
+      if (P.sim && r == (P.rk4 ? 3 : 12)) {  // CheckEvent's predicates on the step's last evaluation
         const double rm3 = V.rm3[s];
         const bool ev = (P.e3 > 0.0 && rm3 < P.e3) || (P.h3 > 0.0 && rm3 > P.h3) ||
                         (P.cf > 0.0 && nn >= 0 && P.cf * (fc.radius[i] + fc.radius[nn]) > __longlong_as_double(rminb));
@@ -451,6 +453,53 @@ __device__ __forceinline__ void stage_input(const View& V, int r, double h) {
     double acc = g_rk_a[r][0] * V.f[(size_t)g_rk_idx[r][0] * ne + e];
     for (int q = 1; q < K; ++q) acc = acc + g_rk_a[r][q] * V.f[(size_t)g_rk_idx[r][q] * ne + e];
     V.yt[e] = V.y0[e] + h * acc;
+  }
+  __syncthreads();
+}
+
+// Simulator::DecisionMaking up to where the host has work
+// (Simulator.cpp:181-250), after an accepted step of S.h_did; thread 0.
+__device__ __forceinline__ void sim_decision(Ctl& S, int any) {
+  sol_sim_line& L = S.L;
+  L.steps += 1;
+  L.elapsed += S.h_did;
+  L.last_save += S.h_did;
+  S.flush = 0;
+  if (any) {
+    S.reason = SOL_STOP_EVENT;
+    S.stop = 1;
+  } else {
+    const double clock = L.relative_end ? L.elapsed : S.t;
+    if (fabs(clock) >= fabs(L.length)) {
+      S.reason = SOL_STOP_LENGTH;
+      S.stop = 1;
+    } else {
+      if (fabs(clock + S.h_next) > fabs(L.length)) S.h_next = L.length - clock;
+      if (fabs(L.last_save) >= fabs(L.output)) {
+        S.reason = SOL_STOP_OUTPUT;
+        S.stop = 1;
+      } else {
+        if (fabs(L.last_save + S.h_next) > fabs(L.output)) S.h_next = L.output - L.last_save;
+        S.flush = (L.steps % 100) == 0;  // Tools::CheckAgainstSmallestNumber every CheckForSM steps
+      }
+    }
+  }
+  S.h = S.h_next;
+}
+
+// An accepted step: y0 <- the new state (flushed below the smallest number
+// when due), written where this CTA owns the body; the step-start state kept
+// when the step stops with an event.
+__device__ __forceinline__ void commit_step(const GroupArgs& P, const View& V, const Ctl& S, int ne, int ns,
+                                            bool home) {
+  const bool keep_start = P.sim && P.yprev && S.stop && S.reason == SOL_STOP_EVENT;
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    double v = V.yn[e];
+    const int s = e / 6;
+    if (keep_start && (s >= ns || home)) P.yprev[6 * V.body[s] + (e - 6 * s)] = V.y0[e];
+    if (S.flush && fabs(v) < 1.0e-50) v = 0.0;
+    V.y0[e] = v;
+    if (s >= ns || home) P.y0[6 * V.body[s] + (e - 6 * s)] = v;
   }
   __syncthreads();
 }
@@ -590,8 +639,13 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
     if (threadIdx.x == 0) {  // Driver: bodyData->h = timeLine->hNext (:74-75)
       S.h = S.h_next;
       S.accepted = 0;
-      // every stage of the step is evaluated at the step's start time
+      // RKF78 evaluates every stage at the step's start time; RK4 at t + c h
+      // (RungeKutta4.cpp:101-116)
       S.factor = fc.gas.present ? sol_reduction_factor(fc.gas, S.t) : 1.0;
+      if (P.rk4) {
+        const double cst[4] = {0.0, 1.0 / 2.0, 1.0 / 2.0, 1.0};
+        for (int q = 0; q < 4; ++q) S.fac[q] = fc.gas.present ? sol_reduction_factor(fc.gas, S.t + cst[q] * S.h) : 1.0;
+      }
     }
     __syncthreads();
     V.factor = S.factor;
@@ -599,6 +653,56 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
     for (int e = threadIdx.x; e < ne; e += blockDim.x) V.yt[e] = V.y0[e];
     __syncthreads();
     evaluate(P, V, S.t, SOL_EVAL_ALL, 0);
+    if (P.rk4) {  // RungeKutta4::Driver and Step (RungeKutta4.cpp:20-129)
+      for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+        const int s = e / 6;
+        if (s >= ns || home) P.accel[6 * V.body[s] + (e - 6 * s)] = V.f[e];
+      }
+      const double h = S.h;
+      const double a[4] = {0.0, 1.0 / 2.0, 1.0 / 2.0, 1.0};  // a21, a32, a43
+      for (int r = 1; r <= 3; ++r) {
+        const double* fp = V.f + (size_t)(r - 1) * ne;
+        for (int e = threadIdx.x; e < ne; e += blockDim.x) V.yt[e] = V.y0[e] + h * (a[r] * fp[e]);
+        __syncthreads();
+        V.factor = S.fac[r];
+        evaluate(P, V, S.t, SOL_EVAL_GAS_DRAG, r);
+      }
+      const double b1 = 1.0 / 6.0, b2 = 1.0 / 3.0, b3 = 1.0 / 3.0, b4 = 1.0 / 6.0;
+      for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+        const double* F = V.f;
+        const double yn = V.y0[e] + h * (b1 * F[e] + b2 * F[(size_t)ne + e] + b3 * F[(size_t)2 * ne + e] +
+                                         b4 * F[(size_t)3 * ne + e]);
+        V.yn[e] = yn;
+        const int s = e / 6;
+        if (s >= ns || home) P.ynew[6 * V.body[s] + (e - 6 * s)] = yn;
+      }
+      int any_ev = 0;
+      if (P.sim) {  // the event flags of every CTA
+        int* evp = P.ev + (size_t)parity * gridDim.x;
+        parity ^= 1;
+        if (threadIdx.x == 0) evp[blockIdx.x] = S.event;
+        ok = group_barrier(P, &S.abort);
+        if (!ok) break;
+        if (threadIdx.x < 32) {
+          for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) any_ev |= gridDim.x > 1 ? __ldcg(evp + b) : S.event;
+          any_ev = (int)__reduce_or_sync(0xFFFFFFFFu, (unsigned)any_ev);
+        }
+      } else {
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        S.h_did = h;
+        S.t += S.h_did;
+        S.h_next = h;  // RK4 keeps its step size (and a clamp of it)
+        S.accepted = 1;
+        S.n_acc++;
+        if (P.sim) sim_decision(S, any_ev);
+        S.event = 0;
+      }
+      __syncthreads();
+      commit_step(P, V, S, ne, ns, home);
+      continue;
+    }
     for (int e = threadIdx.x; e < ne; e += blockDim.x) {
       const double f0 = V.f[e];
       V.ys[e] = fabs(V.y0[e]) + fabs(S.h * f0) + 1.0e-30;
@@ -678,34 +782,7 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
           S.h = S.h_next;
           S.accepted = 1;
           S.n_acc++;
-          if (P.sim) {  // Simulator::DecisionMaking up to where the host has work (Simulator.cpp:181-250)
-            const int any = any_ev;
-            sol_sim_line& L = S.L;
-            L.steps += 1;
-            L.elapsed += S.h_did;
-            L.last_save += S.h_did;
-            S.flush = 0;
-            if (any) {
-              S.reason = SOL_STOP_EVENT;
-              S.stop = 1;
-            } else {
-              const double clock = L.relative_end ? L.elapsed : S.t;
-              if (fabs(clock) >= fabs(L.length)) {
-                S.reason = SOL_STOP_LENGTH;
-                S.stop = 1;
-              } else {
-                if (fabs(clock + S.h_next) > fabs(L.length)) S.h_next = L.length - clock;
-                if (fabs(L.last_save) >= fabs(L.output)) {
-                  S.reason = SOL_STOP_OUTPUT;
-                  S.stop = 1;
-                } else {
-                  if (fabs(L.last_save + S.h_next) > fabs(L.output)) S.h_next = L.output - L.last_save;
-                  S.flush = (L.steps % 100) == 0;  // Tools::CheckAgainstSmallestNumber every CheckForSM steps
-                }
-              }
-            }
-            S.h = S.h_next;
-          }
+          if (P.sim) sim_decision(S, any_ev);
         } else {
           S.n_rej++;
           const double hTemp = 0.9 * h * sol_inv_root<4>(em);
@@ -717,16 +794,7 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
       }
       __syncthreads();
       if (S.accepted) {
-        const bool keep_start = P.sim && P.yprev && S.stop && S.reason == SOL_STOP_EVENT;
-        for (int e = threadIdx.x; e < ne; e += blockDim.x) {
-          double v = V.yn[e];
-          const int s = e / 6;
-          if (keep_start && (s >= ns || home)) P.yprev[6 * V.body[s] + (e - 6 * s)] = V.y0[e];
-          if (S.flush && fabs(v) < 1.0e-50) v = 0.0;
-          V.y0[e] = v;
-          if (s >= ns || home) P.y0[6 * V.body[s] + (e - 6 * s)] = v;
-        }
-        __syncthreads();
+        commit_step(P, V, S, ne, ns, home);
         break;
       }
       if (S.status) break;
@@ -806,16 +874,17 @@ size_t layout(GroupArgs& P, int nsink, int ns) {
 
 }  // namespace
 
-// Whether the system can run its RKF78 driver calls on the group path.
+// Whether the system can run its RKF78 / RK4 driver calls on the group path.
 int sol_group_eligible(const sol_ctx* c) {
   if (c->barycentric) return 0;
   const int ns = c->cls.nm + c->cls.n_spl;
   return ns >= 1 && ns <= kMaxSources && c->n - ns <= 152 * 2 * kMaxLocal;
 }
 
-// n_steps RKF78 driver calls in one cooperative launch of the group kernel.
-// Returns SOL_ERR_STATE (nothing launched) when the system does not fit.
-int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim) {
+// n_steps RKF78 (or, with rk4, RungeKutta4) driver calls in one cooperative
+// launch of the group kernel.  Returns SOL_ERR_STATE (nothing launched) when
+// the system does not fit.
+int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim, int rk4) {
   if (!sol_group_eligible(c)) return SOL_ERR_STATE;
   if (!c->d_persist) {
     const size_t doubles = 2 * 7 * 32 + 4096 + 8;
@@ -869,6 +938,7 @@ int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim) {
   P.ns = ns;
   P.local = local;
   P.n_steps = n_steps;
+  P.rk4 = rk4 ? 1 : 0;
   if (sim) {
     if (grid > kGroupMaxCtas) return SOL_ERR_STATE;
     P.sim = 1;

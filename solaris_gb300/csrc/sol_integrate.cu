@@ -651,11 +651,12 @@ int build_driver_graph(sol_ctx* c, int integrator, DriverGraph& G) {
 int sol_integrator_run(sol_ctx* c, int integrator, int n_steps) {
   // few-source systems: every driver call of the sequence in one cooperative
   // launch (falls through when the grid cannot be co-resident)
+  if ((integrator == SOL_RUNGE_KUTTA_FEHLBERG78 || integrator == SOL_RUNGE_KUTTA4) && c->device_loop &&
+      n_steps > 0 && sol_group_eligible(c)) {
+    const int r = sol_group_rkf78(c, n_steps, nullptr, integrator == SOL_RUNGE_KUTTA4);
+    if (r != SOL_ERR_STATE) return r;
+  }
   if (integrator == SOL_RUNGE_KUTTA_FEHLBERG78 && c->device_loop && n_steps > 0) {
-    if (sol_group_eligible(c)) {
-      const int r = sol_group_rkf78(c, n_steps);
-      if (r != SOL_ERR_STATE) return r;
-    }
     if (sol_persist_eligible(c)) {
       const int r = sol_persist_rkf78(c, n_steps);
       if (r != SOL_ERR_STATE) return r;

@@ -205,7 +205,7 @@ struct GroupSim {
   double* yprev;  // when not null: the state at the start of the step that stops with an event
 };
 constexpr int kGroupMaxCtas = 2048;
-int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim = nullptr);
+int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim = nullptr, int rk4 = 0);
 int sol_fp64_peak_launch(int device, double* flops);
 int sol_check_pair_math_launch(int device, int mode, long long n, unsigned long long seed, long long* result);
 

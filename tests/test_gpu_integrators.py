@@ -120,6 +120,19 @@ def test_rkf78_driver_per_step_mixed_gas():
     _per_step(s, abi.RUNGE_KUTTA_FEHLBERG78, 25, s.h0, exact=False)
 
 
+def test_rk4_driver_per_step_config1():
+    """RK4 driver calls of a few-source system run in the group kernel."""
+    s = scenarios.config1(seed=1503)
+    _per_step(s, abi.RUNGE_KUTTA4, 20, s.h0 * 100, exact=True)
+
+
+def test_rk4_driver_per_step_mixed_gas():
+    """RK4 in the group kernel with drag and type I / II migration (stage times
+    t + c h for the gas factor)."""
+    s = scenarios.mixed_gas_system(seed=3301)
+    _per_step(s, abi.RUNGE_KUTTA4, 15, s.h0 * 100, exact=False)
+
+
 def test_dormand_prince_driver_per_step_config1():
     s = scenarios.config1(seed=1502)
     _per_step(s, abi.DORMAND_PRINCE, 20, s.h0 * 50, exact=True)
