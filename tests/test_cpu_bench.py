@@ -1,0 +1,49 @@
+"""bench.py's reference arm (the reference's CPU path, timed on the host
+cores) keeps the benchmark line's contract: one JSON line on rank 0 with the
+metric, unit and config of the GPU arm, a cpu_baseline describing the run
+and an e2e entry without device copies; under torchrun the other ranks exit
+0 without work."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ARGS = ["--impl", "reference", "--steps", "1", "--warmup", "3"]
+
+
+def _lines(out):
+    return [json.loads(l) for l in out.splitlines() if l.startswith("{")]
+
+
+def _check(line):
+    assert line["impl"] == "reference"
+    assert line["unit"] == "pair interactions/s" and line["value"] > 0
+    assert line["steps"] == 1 and line["warmup"] == 3 and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert "workload" in line["config"]
+
+
+def test_reference_arm_line():
+    r = subprocess.run([sys.executable, "bench.py", *ARGS], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _lines(r.stdout)
+    assert len(lines) == 1
+    _check(lines[0])
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    pytest.importorskip("torch.distributed.run")
+    env = dict(os.environ, MASTER_ADDR="127.0.0.1")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", "29561", "bench.py", "--gpus", "2", *ARGS]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _lines(r.stdout)
+    assert len(lines) == 1  # rank 0 alone prints
+    _check(lines[0])
+    assert lines[0]["n_gpus"] == 2
