@@ -85,6 +85,11 @@ def test_null_arguments(lib):
     assert lib.sol_set_precision(None, 0) == abi.SOL_ERR_ARG
     assert lib.sol_accel_compute(None, 0.0, None, None, None, None, None) == abi.SOL_ERR_ARG
     assert lib.sol_destroy(None) == abi.SOL_OK
+    r = (C.c_int64 * 3)()
+    assert lib.sol_check_pair_math(0, 10, 16, 1, r) == abi.SOL_ERR_ARG   # no such sample family
+    assert lib.sol_check_pair_math(0, -1, 16, 1, r) == abi.SOL_ERR_ARG
+    assert lib.sol_check_pair_math(0, 0, -1, 1, r) == abi.SOL_ERR_ARG
+    assert lib.sol_check_pair_math(0, 0, 16, 1, None) == abi.SOL_ERR_ARG
 
 
 def test_pair_count_matches_oracle_sample():
