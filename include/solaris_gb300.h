@@ -472,8 +472,15 @@ int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_type, const 
                         double* d_nn_dist, int32_t precision, void* stream);
 
 /* ---- measurement helpers ------------------------------------------------ */
-/* Measured FP64 fused-multiply-add throughput of this GPU in FLOP/s (FMA = 2). */
+/* Measured FP64 fused-multiply-add throughput of this GPU in FLOP/s (FMA = 2):
+ * twice rates[0] of sol_measure_fp64_pipe. */
 int sol_measure_fp64_peak(int32_t device, double* flops);
+/* Measured FP64 pipe throughput in thread instructions per second:
+ * rates[0] DFMA, rates[1] DADD, rates[2] DMUL, each from 16 independent
+ * chains per thread on a grid of exactly the CTAs the SMs hold at once (best
+ * of 5 launches of ~30 ms); sm_mhz (may be NULL) receives the SM clock during
+ * the fastest DFMA launch, from clock64() over its event time. */
+int sol_measure_fp64_pipe(int32_t device, double rates[3], double* sm_mhz);
 /* Self-check of the reference-form pair arithmetic: the correctly rounded
  * sqrt(a) and 1 / (a sqrt(a)) that replace IEEE square root and division in
  * every FP64 GravityAC pair (Acceleration.cpp:294-317), and the integer-pipe

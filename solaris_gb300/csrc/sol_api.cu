@@ -919,6 +919,11 @@ int sol_measure_fp64_peak(int32_t device, double* flops) {
   return sol_fp64_peak_launch(device, flops);
 }
 
+int sol_measure_fp64_pipe(int32_t device, double rates[3], double* sm_mhz) {
+  if (!rates) return SOL_ERR_ARG;
+  return sol_fp64_rates_launch(device, rates, sm_mhz);
+}
+
 int sol_check_pair_math(int32_t device, int32_t mode, int64_t n, uint64_t seed, int64_t result[3]) {
   if (!result || mode < 0 || mode > 9 || n < 0) return SOL_ERR_ARG;
   long long r[3];

@@ -77,19 +77,37 @@ __global__ void k_potential(int n, const double* __restrict__ y0, const double* 
   if (i < n) pe[i] = acc;
 }
 
-// Dependent FMA chains: FP64 pipe throughput.
-__global__ void k_dfma_peak(double seed, double b, double* out, int iters) {
-  double v[8];
+// FP64 pipe throughput: kRateChains independent chains of one FP64
+// instruction kind per thread (OP 0 DFMA, 1 DADD, 2 DMUL), a grid of exactly
+// the CTAs the SMs hold at once, so every SM runs the whole time with the
+// same warps.  Thread 0 of CTA 0 records the SM cycles between its first and
+// last chain step: with the launch's event time this gives the SM clock the
+// rate was measured at.  Chains converge (v -> v b + c with b < 1, the sum
+// and product kept near 1): no subnormal or special operand is ever formed.
+constexpr int kRateChains = 16;
+constexpr int kRateThreads = 256;
+
+template <int OP>
+__global__ void __launch_bounds__(kRateThreads) k_fp64_rate(double b, double c, double* out, long long* cycles,
+                                                            int iters) {
+  double v[kRateChains];
 #pragma unroll
-  for (int c = 0; c < 8; ++c) v[c] = seed + threadIdx.x * 1e-9 + c * 1e-3;
+  for (int k = 0; k < kRateChains; ++k) v[k] = 1.0 + threadIdx.x * 1e-12 + k * 1e-6;
+  const long long t0 = clock64();
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
-    for (int c = 0; c < 8; ++c) v[c] = __fma_rn(v[c], b, 1.0000001);
+    for (int k = 0; k < kRateChains; ++k) {
+      if constexpr (OP == 0) v[k] = __fma_rn(v[k], b, c);
+      if constexpr (OP == 1) v[k] = __dadd_rn(v[k], (it & 1) ? c : -c);
+      if constexpr (OP == 2) v[k] = __dmul_rn(v[k], (it & 1) ? b : 1.0 / b);
+    }
   }
+  const long long t1 = clock64();
   double s = 0;
 #pragma unroll
-  for (int c = 0; c < 8; ++c) s += v[c];
+  for (int k = 0; k < kRateChains; ++k) s += v[k];
   if (s == -12345.0) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+  if (blockIdx.x == 0 && threadIdx.x == 0) cycles[0] = t1 - t0;
 }
 
 // Self-check of sol_ref_rinv3 (correctly rounded sqrt and 1 / (a sqrt a))
@@ -258,35 +276,65 @@ int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_pe) {
   return SOL_OK;
 }
 
-int sol_fp64_peak_launch(int device, double* flops) {
-  SOL_CUDA(cudaSetDevice(device));
-  int nsm = 0;
-  SOL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
-  const int threads = 256, blocks = nsm * 8, iters = 4096;
-  double* out = nullptr;
-  SOL_CUDA(cudaMalloc(&out, sizeof(double) * threads * blocks));
+namespace {
+template <int OP>
+int fp64_rate_one(int nsm, double* out, long long* d_cycles, double* rate, double* mhz) {
+  int per_sm = 0;
+  SOL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fp64_rate<OP>, kRateThreads, 0));
+  if (per_sm < 1) per_sm = 1;
+  const int blocks = nsm * per_sm, iters = 8192;
+  const double b = 1.0 - 1.0 / 1048576.0, c = 1.0 / 1048576.0;
   cudaEvent_t e0, e1;
   SOL_CUDA(cudaEventCreate(&e0));
   SOL_CUDA(cudaEventCreate(&e1));
-  k_dfma_peak<<<blocks, threads>>>(1.0, 0.999999, out, 256);  // warm-up
+  k_fp64_rate<OP><<<blocks, kRateThreads>>>(b, c, out, d_cycles, 1024);  // warm-up (clocks ramp)
   SOL_LAUNCHED();
   float best = 1e30f;
-  for (int rep = 0; rep < 3; ++rep) {
+  long long best_cycles = 0;
+  for (int rep = 0; rep < 5; ++rep) {
     SOL_CUDA(cudaEventRecord(e0));
-    k_dfma_peak<<<blocks, threads>>>(1.0, 0.999999, out, iters);
+    k_fp64_rate<OP><<<blocks, kRateThreads>>>(b, c, out, d_cycles, iters);
     SOL_LAUNCHED();
     SOL_CUDA(cudaEventRecord(e1));
     SOL_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
     SOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    if (ms < best) best = ms;
+    if (ms < best) {
+      best = ms;
+      SOL_CUDA(cudaMemcpy(&best_cycles, d_cycles, sizeof(long long), cudaMemcpyDeviceToHost));
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaFree(out);
-  const double fmas = (double)threads * blocks * 8.0 * iters;
-  *flops = 2.0 * fmas / (best * 1e-3);
+  *rate = (double)blocks * kRateThreads * kRateChains * iters / (best * 1e-3);
+  *mhz = (double)best_cycles / (best * 1e-3) / 1e6;
   return SOL_OK;
+}
+}  // namespace
+
+int sol_fp64_rates_launch(int device, double rates[3], double* sm_mhz) {
+  SOL_CUDA(cudaSetDevice(device));
+  int nsm = 0, max_per_sm = 32;
+  SOL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+  double* out = nullptr;
+  long long* cyc = nullptr;
+  SOL_CUDA(cudaMalloc(&out, sizeof(double) * (size_t)nsm * max_per_sm * kRateThreads));
+  SOL_CUDA(cudaMalloc(&cyc, sizeof(long long)));
+  double mhz[3] = {0, 0, 0};
+  int rc = fp64_rate_one<0>(nsm, out, cyc, &rates[0], &mhz[0]);
+  if (rc == SOL_OK) rc = fp64_rate_one<1>(nsm, out, cyc, &rates[1], &mhz[1]);
+  if (rc == SOL_OK) rc = fp64_rate_one<2>(nsm, out, cyc, &rates[2], &mhz[2]);
+  cudaFree(out);
+  cudaFree(cyc);
+  if (rc == SOL_OK && sm_mhz) *sm_mhz = mhz[0];
+  return rc;
+}
+
+int sol_fp64_peak_launch(int device, double* flops) {
+  double rates[3], mhz = 0;
+  const int rc = sol_fp64_rates_launch(device, rates, &mhz);
+  if (rc == SOL_OK) *flops = 2.0 * rates[0];
+  return rc;
 }
 
 int sol_check_pair_math_launch(int device, int mode, long long n, unsigned long long seed, long long* result) {

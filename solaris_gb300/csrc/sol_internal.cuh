@@ -207,6 +207,7 @@ struct GroupSim {
 constexpr int kGroupMaxCtas = 2048;
 int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim = nullptr, int rk4 = 0);
 int sol_fp64_peak_launch(int device, double* flops);
+int sol_fp64_rates_launch(int device, double rates[3], double* sm_mhz);
 int sol_check_pair_math_launch(int device, int mode, long long n, unsigned long long seed, long long* result);
 
 // ---- PTX helpers: bulk copies (TMA engine) with mbarrier completion --------

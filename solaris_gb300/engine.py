@@ -284,6 +284,17 @@ def fp64_peak_flops(device: int = 0) -> float:
     return float(v.value)
 
 
+def fp64_pipe_rates(device: int = 0) -> dict:
+    """FP64 pipe throughput of this GPU (sol_measure_fp64_pipe): thread
+    instructions per second of DFMA, DADD and DMUL chains, and the SM clock
+    (MHz) the DFMA rate was measured at."""
+    lib = abi.load_library()
+    r = (C.c_double * 3)()
+    mhz = C.c_double(0)
+    abi.check(lib, lib.sol_measure_fp64_pipe(int(device), r, C.byref(mhz)))
+    return {"dfma": float(r[0]), "dadd": float(r[1]), "dmul": float(r[2]), "sm_mhz": float(mhz.value)}
+
+
 def check_pair_math(mode: int, n: int, seed: int = 1, device: int = 0) -> dict:
     """Self-check of the correctly rounded sqrt / reciprocal of the FP64 pair
     against IEEE sqrt and division (sol_check_pair_math): mismatches (0 when
