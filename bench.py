@@ -135,18 +135,44 @@ def run_reference(args, rank, world):
     replicas.finalize()
 
 
-def traffic_from_profiles():
-    """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "pair_kernels_config3.md")
+def profile_figures(name="pair_kernels_65536.md"):
+    """`key: value` lines of a committed ncu summary (DRAM bytes per launch,
+    FP64 instructions per pair measured at the bench size)."""
+    p = os.path.join(ROOT, "profiles", name)
+    out = {}
     if not os.path.exists(p):
-        return None
+        return out
     for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        line = line.strip().lstrip("-* ")
+        if ":" in line and line.split(":", 1)[0].replace("_", "").isalnum():
+            k, v = line.split(":", 1)
             try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+                out[k.strip()] = float(v.strip().split()[0].replace(",", ""))
+            except (ValueError, IndexError):
+                pass
+    return out
+
+
+# The FP64 pipe issues 1/16 warp instruction per SM cycle (ncu
+# sm__inst_executed_pipe_fp64.avg.peak_sustained = 0.0625 on the GB300):
+# 2 thread instructions per SM per cycle.
+FP64_LANES_PER_SM_CYCLE = 2.0
+
+
+def fp64_peak(local, clocks):
+    """FP64 instruction peak (thread instructions/s) at the SM clock sampled
+    during the timed region, and the probe's measured chains beside it."""
+    import torch
+    from solaris_gb300 import engine
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    probe = engine.fp64_pipe_rates(local)
+    mhz = (clocks or {}).get("sm_mhz") or probe["sm_mhz"] or 2070.0
+    peak = FP64_LANES_PER_SM_CYCLE * nsm * mhz * 1e6
+    return peak, {"sms": nsm, "sm_mhz": mhz, "lanes_per_sm_cycle": FP64_LANES_PER_SM_CYCLE,
+                  "probe_dfma_per_s": probe["dfma"], "probe_dadd_per_s": probe["dadd"],
+                  "probe_dmul_per_s": probe["dmul"], "probe_sm_mhz": probe["sm_mhz"],
+                  "probe_frac_of_peak": max(probe["dfma"], probe["dadd"], probe["dmul"]) /
+                  (FP64_LANES_PER_SM_CYCLE * nsm * (probe["sm_mhz"] or mhz) * 1e6)}
 
 
 def ensemble_section(local):
@@ -389,13 +415,14 @@ def main():
     ms_launch = {name: ctx.bench_force(p, reps) for name, p, reps in
                  (("split_ff", abi.PRECISION_SPLIT_FF, 5), ("split", abi.PRECISION_SPLIT, 2),
                   ("fp64", abi.PRECISION_FP64, 2))}
-    peak = engine.fp64_peak_flops(local)  # FLOP/s, FMA = 2
-    peak_ops = peak / 2.0                 # FP64 pipe instructions per second
-    # FP64 instructions per pair each form issues; the reference form: 14 in the
-    # pair (correctly rounded sqrt and reciprocal by one FMA remainder each, the
-    # six term multiplies on the integer pipe) and 3 in-order additions at 31
-    # sinks per CTA (3 x 32 / 31)
+    peak_ops, peak_info = fp64_peak(local, ff["clocks"])  # FP64 thread instructions per second
+    # FP64 instructions per pair of each form's arithmetic: SPLIT_FF the 3
+    # displacement subtractions; SPLIT 16 (displacement, r^2, the Newton
+    # correction with G m, the accumulation); the reference form 14 in the pair
+    # (correctly rounded sqrt and reciprocal by one FMA remainder each, the six
+    # term multiplies on the integer pipe) plus the 3 in-order additions
     fp64_ops = {"split_ff": 3, "split": 16, "fp64": 17}
+    prof = profile_figures()
 
     # end to end through the C-ABI: pinned host state in, host state out, every step
     y_host = torch.empty(6 * s.n, dtype=torch.float64, pin_memory=True).numpy()
@@ -423,8 +450,10 @@ def main():
         forms[name] = {"value": rate(r), "unit": UNIT, "ms_per_step": r["ms_per_step"],
                        "kernel_ms_per_launch": ms_launch[name],
                        "fp64_instructions_per_pair": fp64_ops[name],
+                       "fp64_instructions_per_pair_ncu": prof.get(f"{name}_fp64_instructions_per_pair"),
                        "fp64_pipe_frac": pps * fp64_ops[name] / peak_ops,
                        "conventional_tflops": pps * FLOP_PER_PAIR / 1e12,
+                       "conventional_frac_of_fp64_peak": pps * FLOP_PER_PAIR / (2.0 * peak_ops),
                        "energy_drift": r["energy_drift"], "steps": r.get("k")}
         if name in acc:
             forms[name]["max_rel_accel_err"], forms[name]["rms_rel_accel_err"] = acc[name]
@@ -459,9 +488,14 @@ def main():
         "roofline": {"bound": "fp64", "kernel": f"k_pairs<{head_name.upper()}> (pair kernel)",
                      "achieved": pps_head * fp64_ops[head_name] / 1e9, "peak": peak_ops / 1e9, "unit": "Gop/s",
                      "frac": pps_head * fp64_ops[head_name] / peak_ops,
-                     "traffic": traffic_from_profiles(), "fp64_instructions_per_pair": fp64_ops[head_name],
+                     "traffic": prof.get(f"{head_name}_dram_bytes_per_launch"),
+                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the pair kernel and "
+                                     "k_combine at 65,536 bodies (profiles/pair_kernels_65536.md)",
+                     "fp64_instructions_per_pair": fp64_ops[head_name],
                      "kernel_ms_per_launch": ms_launch[head_name],
-                     "peak_source": "measured in-run: FP64 FMA instruction throughput (sol_measure_fp64_peak)"},
+                     "peak_source": "FP64 pipe issue rate, 2 thread instructions per SM cycle (ncu peak_sustained "
+                                    "1/16 warp instruction), x SMs x the SM clock sampled during the timed region",
+                     "peak_detail": peak_info},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * 6 * s.n, "d2h_bytes_per_step": 8 * 6 * s.n,
                 "steps": ke, "api": "sol_driver_host (pinned host y0 in/out)"},

@@ -191,6 +191,8 @@ int sol_gas_component_init(sol_gas_component* gas);
 int sol_create(const sol_body_data* bodies, const sol_gas_component* gas_or_null,
                int32_t barycentric, int32_t device, sol_ctx** out);
 int sol_destroy(sol_ctx* ctx);
+/* sol_precision; a barycentric context (GravityBC_*, FP64 only) rejects the
+ * split forms with SOL_ERR_ARG. */
 int sol_set_precision(sol_ctx* ctx, int32_t precision);
 /* Acceleration::evaluateGasDrag / evaluateTypeIMigration / evaluateTypeIIMigration */
 int sol_set_eval_flags(sol_ctx* ctx, uint32_t flags);
@@ -471,6 +473,29 @@ int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_type, const 
                         const double* d_y, double* d_dydt, double* d_rm3, int32_t* d_nn_idx,
                         double* d_nn_dist, int32_t precision, void* stream);
 
+/* The status of the last sol_gravity_noalloc call on the current device,
+ * read after the work queued on `stream` has finished (this call waits for
+ * that stream): SOL_OK, or SOL_ERR_TIMEOUT when a bounded wait of that
+ * evaluation ran out, in which case its outputs are incomplete.  *status
+ * (may be NULL) receives the raw device status word.  Allocates nothing.
+ * No counterpart in the reference. */
+int sol_gravity_noalloc_status(void* stream, int32_t* status);
+
+/* ---- failure-path test hooks --------------------------------------------
+ * Every device wait (a bulk copy's mbarrier phase, the group driver's
+ * barrier) polls at most a spin limit of times; a wait that runs out raises
+ * SOL_DEV_TIMEOUT and the call returns SOL_ERR_TIMEOUT, leaving the context
+ * usable.  This hook lets a test reach that path without faulting anything:
+ * spin_limit bounds the waits (0: the default of 2^26 polls) and withhold >= 0
+ * names a participant that never arrives (-1: none).
+ *  ctx != NULL: the context's group driver (few-source RKF78 / RK4 systems in
+ *    sol_driver and sol_run_until): CTA `withhold` skips its arrivals at the
+ *    group barrier, so the other CTAs' waits run out.
+ *  ctx == NULL: sol_gravity_noalloc, process-wide: source tile `withhold` of
+ *    every CTA is never copied, so the wait for it runs out.
+ * No counterpart in the reference. */
+int sol_set_wait_test(sol_ctx* ctx, uint32_t spin_limit, int32_t withhold);
+
 /* ---- measurement helpers ------------------------------------------------ */
 /* Measured FP64 fused-multiply-add throughput of this GPU in FLOP/s (FMA = 2):
  * twice rates[0] of sol_measure_fp64_pipe. */
@@ -478,8 +503,10 @@ int sol_measure_fp64_peak(int32_t device, double* flops);
 /* Measured FP64 pipe throughput in thread instructions per second:
  * rates[0] DFMA, rates[1] DADD, rates[2] DMUL, each from 16 independent
  * chains per thread on a grid of exactly the CTAs the SMs hold at once (best
- * of 5 launches of ~30 ms); sm_mhz (may be NULL) receives the SM clock during
- * the fastest DFMA launch, from clock64() over its event time. */
+ * of 5 launches of ~50 ms); sm_mhz (may be NULL) receives the SM clock during
+ * the fastest DFMA launch (SM cycles over %globaltimer nanoseconds in one
+ * CTA).  On the GB300 such chains reach 84% of the FP64 pipe's issue rate
+ * (1/16 warp instruction per SM cycle). */
 int sol_measure_fp64_pipe(int32_t device, double rates[3], double* sm_mhz);
 /* Self-check of the reference-form pair arithmetic: the correctly rounded
  * sqrt(a) and 1 / (a sqrt(a)) that replace IEEE square root and division in

@@ -271,6 +271,7 @@ int sol_create(const sol_body_data* b, const sol_gas_component* gas, int32_t bar
   c->eval_flags = SOL_EVAL_ALL;
   c->eps = pow(10, -10.0);  // RungeKuttaFehlberg78.cpp:38-39
   c->device_loop = 1;
+  c->test_skip_cta = -1;
   c->has_gas = gas != nullptr;
   if (gas) c->gas_host = *gas;
   Classes& cl = c->cls;
@@ -385,6 +386,11 @@ int sol_set_precision(sol_ctx* c, int32_t p) {
   RET(check_ctx(c));
   if (p != SOL_PRECISION_FP64 && p != SOL_PRECISION_SPLIT && p != SOL_PRECISION_SPLIT_FF) {
     sol_set_error("unknown precision %d", p);
+    return SOL_ERR_ARG;
+  }
+  if (p != SOL_PRECISION_FP64 && c->barycentric) {
+    // GravityBC_* (Acceleration.cpp:541-634) has only the reference form here
+    sol_set_error("precision %d: barycentric contexts compute in FP64 only", p);
     return SOL_ERR_ARG;
   }
   if (p != SOL_PRECISION_FP64 && !c->barycentric && !c->d_part && sol_force_uses_chunk_partials(c)) {
@@ -917,6 +923,20 @@ int sol_bench_force(sol_ctx* c, int32_t precision, int32_t reps, double* ms_per_
 int sol_measure_fp64_peak(int32_t device, double* flops) {
   if (!flops) return SOL_ERR_ARG;
   return sol_fp64_peak_launch(device, flops);
+}
+
+int sol_set_wait_test(sol_ctx* c, uint32_t spin_limit, int32_t withhold) {
+  if (withhold < -1) {
+    sol_set_error("sol_set_wait_test: withhold must be -1 (none) or an index");
+    return SOL_ERR_ARG;
+  }
+  if (!c) {
+    sol_noalloc_wait_test(spin_limit, withhold);
+    return SOL_OK;
+  }
+  c->test_spin = spin_limit;
+  c->test_skip_cta = withhold;
+  return SOL_OK;
 }
 
 int sol_measure_fp64_pipe(int32_t device, double rates[3], double* sm_mhz) {

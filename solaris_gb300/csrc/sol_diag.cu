@@ -79,11 +79,13 @@ __global__ void k_potential(int n, const double* __restrict__ y0, const double* 
 
 // FP64 pipe throughput: kRateChains independent chains of one FP64
 // instruction kind per thread (OP 0 DFMA, 1 DADD, 2 DMUL), a grid of exactly
-// the CTAs the SMs hold at once, so every SM runs the whole time with the
-// same warps.  Thread 0 of CTA 0 records the SM cycles between its first and
-// last chain step: with the launch's event time this gives the SM clock the
-// rate was measured at.  Chains converge (v -> v b + c with b < 1, the sum
-// and product kept near 1): no subnormal or special operand is ever formed.
+// the CTAs the SMs hold at once.  Thread 0 of CTA 0 records the SM cycles
+// (clock64) and the nanoseconds (%globaltimer) between its first and last
+// chain step: their ratio is the SM clock the rate was measured at.  (The
+// CTA's own duration is not the launch's: the warp schedulers favour the
+// oldest warps, so the CTAs of an SM largely finish one after another.)
+// Chains converge (v -> v b + c with b < 1, the sum and product kept near
+// 1): no subnormal or special operand is ever formed.
 constexpr int kRateChains = 16;
 constexpr int kRateThreads = 256;
 
@@ -94,6 +96,8 @@ __global__ void __launch_bounds__(kRateThreads) k_fp64_rate(double b, double c, 
 #pragma unroll
   for (int k = 0; k < kRateChains; ++k) v[k] = 1.0 + threadIdx.x * 1e-12 + k * 1e-6;
   const long long t0 = clock64();
+  unsigned long long g0 = 0, g1 = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
     for (int k = 0; k < kRateChains; ++k) {
@@ -103,11 +107,15 @@ __global__ void __launch_bounds__(kRateThreads) k_fp64_rate(double b, double c, 
     }
   }
   const long long t1 = clock64();
+  if (blockIdx.x == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
   double s = 0;
 #pragma unroll
   for (int k = 0; k < kRateChains; ++k) s += v[k];
   if (s == -12345.0) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-  if (blockIdx.x == 0 && threadIdx.x == 0) cycles[0] = t1 - t0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cycles[0] = t1 - t0;
+    cycles[1] = (long long)(g1 - g0);
+  }
 }
 
 // Self-check of sol_ref_rinv3 (correctly rounded sqrt and 1 / (a sqrt a))
@@ -290,7 +298,7 @@ int fp64_rate_one(int nsm, double* out, long long* d_cycles, double* rate, doubl
   k_fp64_rate<OP><<<blocks, kRateThreads>>>(b, c, out, d_cycles, 1024);  // warm-up (clocks ramp)
   SOL_LAUNCHED();
   float best = 1e30f;
-  long long best_cycles = 0;
+  long long best_cycles[2] = {0, 1};
   for (int rep = 0; rep < 5; ++rep) {
     SOL_CUDA(cudaEventRecord(e0));
     k_fp64_rate<OP><<<blocks, kRateThreads>>>(b, c, out, d_cycles, iters);
@@ -301,13 +309,13 @@ int fp64_rate_one(int nsm, double* out, long long* d_cycles, double* rate, doubl
     SOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     if (ms < best) {
       best = ms;
-      SOL_CUDA(cudaMemcpy(&best_cycles, d_cycles, sizeof(long long), cudaMemcpyDeviceToHost));
+      SOL_CUDA(cudaMemcpy(best_cycles, d_cycles, 2 * sizeof(long long), cudaMemcpyDeviceToHost));
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *rate = (double)blocks * kRateThreads * kRateChains * iters / (best * 1e-3);
-  *mhz = (double)best_cycles / (best * 1e-3) / 1e6;
+  *mhz = best_cycles[1] > 0 ? 1e3 * (double)best_cycles[0] / (double)best_cycles[1] : 0.0;
   return SOL_OK;
 }
 }  // namespace
@@ -319,7 +327,7 @@ int sol_fp64_rates_launch(int device, double rates[3], double* sm_mhz) {
   double* out = nullptr;
   long long* cyc = nullptr;
   SOL_CUDA(cudaMalloc(&out, sizeof(double) * (size_t)nsm * max_per_sm * kRateThreads));
-  SOL_CUDA(cudaMalloc(&cyc, sizeof(long long)));
+  SOL_CUDA(cudaMalloc(&cyc, 2 * sizeof(long long)));
   double mhz[3] = {0, 0, 0};
   int rc = fp64_rate_one<0>(nsm, out, cyc, &rates[0], &mhz[0]);
   if (rc == SOL_OK) rc = fp64_rate_one<1>(nsm, out, cyc, &rates[1], &mhz[1]);

@@ -14,6 +14,7 @@
 //                 epilogue adds gas drag and type-I/II migration for the sink.
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 
 #include "sol_internal.cuh"
@@ -202,10 +203,12 @@ __device__ __forceinline__ void two_sum(double& s, double& c, double a) {
   c += err;
 }
 
+// spin: the limit of every mbarrier wait; withhold >= 0: that tile is never
+// copied, so its wait runs out (failure-path tests only; -1 in production).
 template <int PREC>
 __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const double* __restrict__ y,
                                                            double* __restrict__ dydt, TimeSpec ts, uint32_t flags,
-                                                           int* dev_status) {
+                                                           int* dev_status, uint32_t spin, int withhold) {
   constexpr int NARR = (PREC == SOL_PRECISION_FP64) ? 7 : 4;
   __shared__ __align__(128) TileSmem<NARR> sm;
   const Classes& c = fc.cls;
@@ -231,8 +234,8 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (ntiles > 0) issue_tile<NARR>(sm, fc.src, fc.npad, 0, 0);
-    if (ntiles > 1) issue_tile<NARR>(sm, fc.src, fc.npad, 1, 1);
+    if (ntiles > 0 && withhold != 0) issue_tile<NARR>(sm, fc.src, fc.npad, 0, 0);
+    if (ntiles > 1 && withhold != 1) issue_tile<NARR>(sm, fc.src, fc.npad, 1, 1);
   }
 
   double ax = 0.0, ay = 0.0, az = 0.0;  // FP64: running sums; SPLIT: tile partials
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
   for (; t < ntiles; ++t) {
     const int st = t & 1;
     const uint32_t parity = (t >> 1) & 1;
-    const bool ok = sol_mbar_wait(&sm.bar[st], parity);
+    const bool ok = sol_mbar_wait_n(&sm.bar[st], parity, spin);
     const int j0 = t * kTile;
     const int jmax = min(kTile, ns_cta - j0);  // sources beyond the CTA's range are never read
     if (ok && i < n && i >= 1) {
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
     }
     if (threadIdx.x == 0 && t + 2 < ntiles) {
       sol_fence_proxy_async();
-      issue_tile<NARR>(sm, fc.src, fc.npad, t + 2, st);
+      if (t + 2 != withhold) issue_tile<NARR>(sm, fc.src, fc.npad, t + 2, st);
     }
     if (t + 2 < ntiles) issued = t + 3;
   }
@@ -281,7 +284,7 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
     if (threadIdx.x == 0) {
       atomicOr(dev_status, SOL_DEV_TIMEOUT);
       // drain the copies still in flight (bounded) before the CTA exits
-      for (int u = t; u < issued; ++u) sol_mbar_wait(&sm.bar[u & 1], (u >> 1) & 1);
+      for (int u = t; u < issued; ++u) sol_mbar_wait_n(&sm.bar[u & 1], (u >> 1) & 1, spin);
     }
     __syncthreads();
     return;
@@ -1196,7 +1199,7 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
     k_combine<<<(c->n + 255) / 256, 256, 0, c->stream>>>(fc, d_y, d_dydt, c->d_part, nchunk, ts, flags);
   } else {
     k_gravity_ac<SOL_PRECISION_FP64><<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags,
-                                                                       &c->d_ctrl->dev_status);
+                                                                       &c->d_ctrl->dev_status, SOL_SPIN_LIMIT, -1);
   }
   SOL_LAUNCHED();
   return SOL_OK;
@@ -1238,9 +1241,16 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 namespace {
 std::mutex g_noalloc_mu;
 double* g_noalloc_addr[64];  // device address of g_noalloc_scratch, per device ordinal
+// failure-path test hook (sol_set_wait_test with no context): the mbarrier
+// spin limit of the next calls (0: SOL_SPIN_LIMIT) and a tile never copied
+std::atomic<unsigned> g_noalloc_spin{0};
+std::atomic<int> g_noalloc_withhold{-1};
 
 // Host code cannot use g_noalloc_scratch as a device address: resolve it once
-// per device, with that device current.
+// per device, with that device current.  The same first call loads every
+// kernel instance this entry point launches (with CUDA's lazy module loading
+// a kernel's first launch would otherwise load it then), so later calls --
+// of either precision -- do no loading work.
 int noalloc_scratch(double** out) {
   int dev = 0;
   SOL_CUDA(cudaGetDevice(&dev));
@@ -1253,12 +1263,40 @@ int noalloc_scratch(double** out) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return sol_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    cudaFuncAttributes fa;
+    SOL_CUDA(cudaFuncGetAttributes(&fa, k_prepass));
+    SOL_CUDA(cudaFuncGetAttributes(&fa, k_ind_reduce));
+    SOL_CUDA(cudaFuncGetAttributes(&fa, k_gravity_ac<SOL_PRECISION_FP64>));
+    SOL_CUDA(cudaFuncGetAttributes(&fa, k_gravity_ac<SOL_PRECISION_SPLIT>));
     g_noalloc_addr[dev] = (double*)p;
   }
   *out = g_noalloc_addr[dev];
   return SOL_OK;
 }
+
+int* noalloc_status_word(double* scratch) { return (int*)(scratch + kNoAllocSrc + kNoAllocPart + 8); }
 }  // namespace
+
+void sol_noalloc_wait_test(unsigned spin_limit, int withhold_tile) {
+  g_noalloc_spin.store(spin_limit);
+  g_noalloc_withhold.store(withhold_tile);
+}
+
+extern "C" int sol_gravity_noalloc_status(void* stream, int32_t* status) {
+  double* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != SOL_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  int word = 0;
+  SOL_CUDA(cudaMemcpyAsync(&word, noalloc_status_word(scratch), sizeof(int), cudaMemcpyDeviceToHost, st));
+  SOL_CUDA(cudaStreamSynchronize(st));
+  if (status) *status = word;
+  if (word & SOL_DEV_TIMEOUT) {
+    sol_set_error("sol_gravity_noalloc: a bounded device wait ran out; the outputs of that call are incomplete");
+    return SOL_ERR_TIMEOUT;
+  }
+  return SOL_OK;
+}
 
 extern "C" int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_type, const double* d_mass,
                                    const double* d_y, double* d_dydt, double* d_rm3, int32_t* d_nn_idx,
@@ -1316,7 +1354,7 @@ extern "C" int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_t
   fc.ind_part = scratch + kNoAllocSrc;
   fc.ind_sum = scratch + kNoAllocSrc + kNoAllocPart;
   fc.n_ind_blocks = (fc.npad + kPrepassBlock - 1) / kPrepassBlock;
-  int* status = (int*)(scratch + kNoAllocSrc + kNoAllocPart + 8);
+  int* status = noalloc_status_word(scratch);
   // The array keeps the previous call's contents: the source table and the
   // partials are rewritten in full below, the status word must start at zero.
   SOL_CUDA(cudaMemsetAsync(status, 0, sizeof(int), st));
@@ -1332,10 +1370,13 @@ extern "C" int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_t
   }
   TimeSpec ts{nullptr, nullptr, 0.0, 0.0};
   const int nb = (int)((n + kSinkBlock - 1) / kSinkBlock);
+  const unsigned spin_hook = g_noalloc_spin.load();
+  const unsigned spin = spin_hook ? spin_hook : SOL_SPIN_LIMIT;
+  const int withhold = g_noalloc_withhold.load();
   if (split)
-    k_gravity_ac<SOL_PRECISION_SPLIT><<<nb, kSinkBlock, 0, st>>>(fc, d_y, d_dydt, ts, 0u, status);
+    k_gravity_ac<SOL_PRECISION_SPLIT><<<nb, kSinkBlock, 0, st>>>(fc, d_y, d_dydt, ts, 0u, status, spin, withhold);
   else
-    k_gravity_ac<SOL_PRECISION_FP64><<<nb, kSinkBlock, 0, st>>>(fc, d_y, d_dydt, ts, 0u, status);
+    k_gravity_ac<SOL_PRECISION_FP64><<<nb, kSinkBlock, 0, st>>>(fc, d_y, d_dydt, ts, 0u, status, spin, withhold);
   SOL_LAUNCHED();
   return SOL_OK;
 }

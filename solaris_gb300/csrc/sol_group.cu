@@ -28,7 +28,8 @@
 //
 // The group barrier spins on a generation counter with an iteration limit; a
 // CTA that runs out raises SOL_DEV_TIMEOUT and an abort flag that makes every
-// other CTA leave at its next barrier.
+// other CTA leave at its next barrier.  (sol_set_wait_test lowers the limit
+// and can keep one CTA from arriving, so that tests reach this path.)
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -70,6 +71,8 @@ struct GroupArgs {
   unsigned* bar_count;  // group barrier
   unsigned* bar_gen;
   int* abort_flag;
+  unsigned spin;        // spin limit of the group barrier
+  int skip_cta;         // failure-path tests: this CTA never arrives (-1: none)
   sol_ctrl* ctrl;
   int n;
   int ns;               // sources: nm + n_spl
@@ -92,13 +95,13 @@ __device__ bool group_barrier(const GroupArgs& P, int* s_abort) {
     volatile unsigned* gen = P.bar_gen;
     const unsigned g = *gen;
     __threadfence();
-    if (atomicAdd(P.bar_count, 1u) == gridDim.x - 1) {
+    if ((int)blockIdx.x != P.skip_cta && atomicAdd(P.bar_count, 1u) == gridDim.x - 1) {
       *P.bar_count = 0;
       __threadfence();
       atomicAdd(P.bar_gen, 1u);
     } else {
       bool ok = false;
-      for (uint32_t k = 0; k < SOL_SPIN_LIMIT; ++k) {
+      for (uint32_t k = 0; k < P.spin; ++k) {
         if (*gen != g) {
           ok = true;
           break;
@@ -933,6 +936,8 @@ int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim, int rk4) {
   P.bar_count = words;
   P.bar_gen = words + 1;
   P.abort_flag = reinterpret_cast<int*>(words + 2);
+  P.spin = c->test_spin ? c->test_spin : SOL_SPIN_LIMIT;
+  P.skip_cta = c->test_skip_cta;
   P.ctrl = c->d_ctrl;
   P.n = c->n;
   P.ns = ns;

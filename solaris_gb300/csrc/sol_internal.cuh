@@ -171,6 +171,10 @@ struct sol_ctx {
   void* d_sim;             // the step loop's line, stop reason and event flags (sol_run_until)
   double* d_ystart;        // the state at the start of the last step of sol_run_until (collision records)
   int32_t* h_id;           // BodyData::id on the host (output records carry ids)
+  // failure-path test hooks (sol_set_wait_test): the group barrier's spin
+  // limit (0: SOL_SPIN_LIMIT) and a CTA that skips its arrivals (-1: none)
+  unsigned test_spin;
+  int test_skip_cta;
 };
 
 // ---- launch helpers (defined in sol_force.cu / sol_integrate.cu) --------------
@@ -207,6 +211,7 @@ struct GroupSim {
 constexpr int kGroupMaxCtas = 2048;
 int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim = nullptr, int rk4 = 0);
 int sol_fp64_peak_launch(int device, double* flops);
+void sol_noalloc_wait_test(unsigned spin_limit, int withhold_tile);
 int sol_fp64_rates_launch(int device, double rates[3], double* sm_mhz);
 int sol_check_pair_math_launch(int device, int mode, long long n, unsigned long long seed, long long* result);
 
@@ -250,6 +255,25 @@ __device__ __forceinline__ uint32_t sol_mbar_try_wait(uint64_t* bar, uint32_t pa
 __device__ __forceinline__ bool sol_mbar_wait(uint64_t* bar, uint32_t parity) {
   for (uint32_t k = 0; k < SOL_SPIN_LIMIT; ++k)
     if (sol_mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// The same with a caller-given limit (failure-path tests lower it); every
+// poll suspends the thread for at most ~1 us (suspendTimeHint, ns), so the
+// limit also bounds the wait's duration: 2^26 polls ~ 1 min at most, 4,096
+// polls ~ 4 ms.
+__device__ __forceinline__ uint32_t sol_mbar_try_wait_1us(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 1000;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(sol_smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok;
+}
+__device__ __forceinline__ bool sol_mbar_wait_n(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  for (uint32_t k = 0; k < limit; ++k)
+    if (sol_mbar_try_wait_1us(bar, parity)) return true;
   return false;
 }
 

@@ -64,6 +64,12 @@ class Context:
     def set_tolerance(self, eps: float):
         abi.check(self.lib, self.lib.sol_set_tolerance(self.h, float(eps)))
 
+    def set_wait_test(self, spin_limit: int, withhold: int):
+        """Failure-path test hook (sol_set_wait_test): the group driver's
+        barrier gives up after spin_limit polls (0: default) and CTA
+        `withhold` never arrives (-1: none)."""
+        abi.check(self.lib, self.lib.sol_set_wait_test(self.h, int(spin_limit), int(withhold)))
+
     # -- force ----------------------------------------------------------------
     def accel(self, t, y, flags=abi.EVAL_ALL):
         self.set_eval_flags(flags)

@@ -218,7 +218,8 @@ sol_ctx* context(Acceleration* acc, bool bary) {
     sd.gamma_epstein = s.dbls.data() + 6 * n;
     sol_ctx* ctx = nullptr;
     if (sol_create(&sd, has_gas ? &s.gas : nullptr, bary ? 1 : 0, env_device(), &ctx) != SOL_OK) return nullptr;
-    if (sol_set_precision(ctx, precision) != SOL_OK) {
+    // barycentric contexts have the FP64 form only
+    if (sol_set_precision(ctx, bary ? SOL_PRECISION_FP64 : precision) != SOL_OK) {
       sol_destroy(ctx);
       return nullptr;
     }

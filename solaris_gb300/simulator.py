@@ -57,7 +57,9 @@ class EngineBackend:
     """A device context driven one accepted step at a time."""
 
     def __init__(self, system, st, directory: str, device: int = 0, precision: int = abi.PRECISION_FP64):
-        self.ctx = engine.Context(system, device=device, precision=precision)
+        # barycentric frames (GravityBC_*) have the FP64 form only
+        prec = abi.PRECISION_FP64 if system.barycentric else precision
+        self.ctx = engine.Context(system, device=device, precision=prec)
         self.ctx.set_state(system.y0)
         self.integrator = st.integrator
         self.out = engine.Output(self.ctx, os.path.join(directory, st.phases), os.path.join(directory, st.integrals))

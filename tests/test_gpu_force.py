@@ -235,3 +235,20 @@ def test_fp64_fallback_paths_bit_identical(n):
     assert np.array_equal(bits(rm3), bits(rm3_o))
     assert np.array_equal(nn, nn_o) and np.array_equal(bits(nd), bits(nd_o))
     assert nn[5] == 7 and nn[7] == 5
+
+
+def test_barycentric_context_rejects_the_split_forms():
+    """GravityBC_* has only the reference (FP64) form here: a barycentric
+    context refuses SPLIT and SPLIT_FF with SOL_ERR_ARG instead of silently
+    computing in FP64, and keeps evaluating bit for bit afterwards."""
+    d = load("accel_mixed_gas_bc")
+    s = system_from(d)
+    with engine.Context(s, precision=abi.PRECISION_FP64) as ctx:
+        for p in SPLITS:
+            with pytest.raises(abi.SolError) as err:
+                ctx.set_precision(p)
+            assert err.value.code == abi.SOL_ERR_ARG
+            assert "barycentric" in str(err.value)
+        dydt, *_ = ctx.accel(float(d["meta_t"]), s.y0, int(d["meta_flags"]))
+    g = gas_bodies(s)
+    assert np.array_equal(bits(dydt.reshape(-1, 6)[~g]), bits(d["out_dydt"].reshape(-1, 6)[~g]))
