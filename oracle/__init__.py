@@ -257,11 +257,13 @@ class ScenarioBackend:
         self.integrator = st.integrator
         self.phases = os.path.join(directory, st.phases)
         self.integrals_path = os.path.join(directory, st.integrals)
+        self.rejected = 0
 
     def step(self, time, h_next):
         r = self.o.driver(self.integrator, self.y0, time, h_next, 1)
         if r["status"] != 0:
             raise RuntimeError(f"oracle driver status {r['status']}")
+        self.rejected += r["stats"][1]
         self.y0 = r["y0"]
         t, hn, hd = r["tl"]
         return t, hd, hn

@@ -64,11 +64,13 @@ class EngineBackend:
         self.integrator = st.integrator
         self.out = engine.Output(self.ctx, os.path.join(directory, st.phases), os.path.join(directory, st.integrals))
         self.tl = abi.SolTimeLine(0.0, 0.0, 0.0)
+        self.rejected = 0  # attempts the step-size control rejected
 
     def step(self, time: float, h_next: float):
         """One Driver call: returns (time, h_did, h_next)."""
         self.tl.time, self.tl.h_next, self.tl.h_did = time, h_next, 0.0
         r = self.ctx.driver(self.integrator, time, h_next, 1, time_line=self.tl)
+        self.rejected += r["stats"][1]
         return r["time"], r["h_did"], r["h_next"]
 
     def events(self, time, ejection, hit_centrum, collision_factor):
@@ -83,7 +85,8 @@ class EngineBackend:
                               last_save=clock.save if rel else tl.last_save, steps=sim.steps,
                               relative_end=1 if rel else 0)
         factor = st.collision if st.collision is not None else 0.0
-        reason, _ = self.ctx.run_until(self.integrator, line, max_steps, st.ejection, st.hit_centrum, factor)
+        reason, stats = self.ctx.run_until(self.integrator, line, max_steps, st.ejection, st.hit_centrum, factor)
+        self.rejected += stats[1]
         tl.time, tl.h_next, tl.h_did = line.time, line.h_next, line.h_did
         if rel:
             clock.all, clock.save = line.elapsed, line.last_save
@@ -281,6 +284,7 @@ class Simulator:
         self.props = _Properties(self.dir, scenario.settings)
         self.event_id = 0
         self.steps = 0      # Counter::succededStep, over the whole run
+        self.rejected = 0   # attempts rejected by the step-size control (the reference does not count them)
         self.phases = 0
         self.affairs = []
         self.be = None
@@ -403,6 +407,7 @@ class Simulator:
             be.save_phases(tl.time)
             be.save_integrals(tl.time)
         finally:
+            self.rejected += getattr(be, "rejected", 0)
             be.close()
             self.be = None
 
@@ -493,8 +498,8 @@ class Simulator:
         if st.length != 0.0:
             self._log("The main-integration phase of the simulation begins")
             self._main_integration(main)
-        return dict(steps=self.steps, phases=self.phases, time=main.time, affairs=self.affairs,
-                    seconds=_time.time() - t_wall)
+        return dict(steps=self.steps, rejected=self.rejected, phases=self.phases, time=main.time,
+                    affairs=self.affairs, seconds=_time.time() - t_wall)
 
 
 def run_file(path: str, directory: str | None = None, device: int = 0, precision: int = abi.PRECISION_FP64) -> dict:

@@ -298,3 +298,23 @@ def test_guid_layout():
     g = sim._guid_bytes("00112233-4455-6677-8899-aabbccddeeff")
     assert g == bytes([0x33, 0x22, 0x11, 0x00, 0x55, 0x44, 0x77, 0x66, 0x88, 0x99, 0xaa, 0xbb, 0xcc, 0xdd, 0xee, 0xff])
     assert sim._guid_bytes("") == bytes(16)
+
+
+def test_config1_full_length_matches_the_reference_program(tmp_path):
+    """The 256-body RKF78 configuration over its full 1,000 years
+    (tests/golden/make_config1.py): the oracle-driven simulator writes the
+    reference program's integrals and ejection records byte for byte, with
+    its number of accepted steps (driver calls) and rejected attempts (from
+    the program's force-evaluation count)."""
+    import json
+    name = "config1_1000yr"
+    summary = json.load(open(os.path.join(golden_dir(name), "summary.json")))
+    sc = sx.load(xml_path(name))
+    r = sim.Simulator(sc, directory=str(tmp_path), backend=oracle.ScenarioBackend).run()
+    assert (r["steps"], r["rejected"]) == (summary["accepted"], summary["rejected"])
+    assert len(r["affairs"]) == len(summary["events"])
+    for fn in ("Integrals.dat", "TwoBodyAffair.dat"):
+        with open(os.path.join(golden_dir(name), fn), "rb") as f:
+            want = f.read()
+        with open(os.path.join(str(tmp_path), fn), "rb") as f:
+            assert f.read() == want, fn
