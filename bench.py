@@ -220,19 +220,20 @@ def ensemble_section(local):
 
 
 def adjoint_section(local):
-    """Discrete adjoint of fixed-step RKF78 on the adjoint workload (1 star +
-    8 planets + 1,024 planetesimals typed ProtoPlanet, h = shortest period /
-    500): forward and backward milliseconds per step with a checkpoint every
-    100 steps, the backward / forward cost ratio (bound 4), FP64 and SPLIT_FF
-    forces; the oracle's forward step on one core beside it."""
+    """Discrete adjoint of fixed-step RKF78 on the adjoint workload at its
+    full length (1 star + 8 planets + 1,024 planetesimals typed ProtoPlanet,
+    h = shortest period / 500, 10^4 steps, a checkpoint every 100): forward
+    and backward milliseconds per step, the backward / forward cost ratio
+    (bound 4), FP64 and SPLIT_FF forces; the oracle's forward step on one core
+    beside it."""
     import numpy as np
 
     import oracle
     from solaris_gb300 import engine, scenarios
     s = scenarios.config5()
-    h, n_steps, every = s.h0 * 100, 1000, 100
+    h, n_steps, every = s.h0 * 100, 10000, 100
     out = {"workload": "1 star + 8 planets + 1,024 ProtoPlanet planetesimals, fixed-step RKF78, "
-                       "h = shortest period / 500, checkpoint every 100 steps",
+                       "h = shortest period / 500, 10^4 steps, checkpoint every 100 steps",
            "n_bodies": s.n, "steps": n_steps, "checkpoint_every": every,
            "pairs_per_step": 11 * s.pair_count()}
     rng = np.random.default_rng(1005)
@@ -248,10 +249,9 @@ def adjoint_section(local):
             t0 = time.perf_counter()
             ctx.adjoint_backward(g.reshape(-1))
             tb = time.perf_counter() - t0
-        out[name] = {"forward_ms_per_step": 1e3 * tf / n_steps, "backward_ms_per_step": 1e3 * tb / n_steps,
-                     "backward_over_forward": tb / tf,
-                     "forward_pairs_per_s": out["pairs_per_step"] * n_steps / tf,
-                     "projected_s_for_10000_steps": (tf + tb) * 10000 / n_steps}
+        out[name] = {"forward_s": tf, "backward_s": tb, "forward_ms_per_step": 1e3 * tf / n_steps,
+                     "backward_ms_per_step": 1e3 * tb / n_steps, "backward_over_forward": tb / tf,
+                     "forward_pairs_per_s": out["pairs_per_step"] * n_steps / tf}
     o = oracle.Oracle(s)
     k = 3
     t0 = time.perf_counter()
@@ -261,38 +261,92 @@ def adjoint_section(local):
     return out
 
 
+def config1_full_run(local):
+    """The 256-body configuration over its full 1,000 years as the scenario
+    file tests/golden/scenarios/config1_1000yr.xml: the device simulator, the
+    oracle-driven simulator on one host core (its output files are the
+    reference program's byte for byte), and the reference program's own run
+    of the file (tests/golden/scenarios/config1_1000yr/summary.json: driver
+    calls and force evaluations counted around its unchanged objects, wall
+    time on the x86 machine that generated it)."""
+    import tempfile
+
+    import oracle
+    from solaris_gb300 import scenario_xml, simulator
+    xml = os.path.join(ROOT, "tests", "golden", "scenarios", "config1_1000yr.xml")
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "scenarios", "config1_1000yr", "summary.json")))
+
+    def run(backend=None):
+        sc = scenario_xml.load(xml)
+        with tempfile.TemporaryDirectory() as d:
+            kw = {"backend": backend} if backend else {"device": local}
+            t0 = time.perf_counter()
+            r = simulator.Simulator(sc, directory=d, **kw).run()
+            wall = time.perf_counter() - t0
+            integ = open(os.path.join(d, "Integrals.dat"), "rb").read()
+        e = _energies(integ)
+        return {"wall_s": wall, "accepted": r["steps"], "rejected": r["rejected"],
+                "steps_per_s": r["steps"] / wall, "events": len(r["affairs"]),
+                "ejected_ids": sorted(int(a["id2"]) for a in r["affairs"]),
+                "energy_rel_drift": abs((e[-1] - e[0]) / e[0])}
+
+    gpu = run()
+    cpu = run(oracle.ScenarioBackend)
+    cpu.update(kind="port", cores=1, sample="the full run, oracle-driven simulator (the reference's bytes)")
+    want = set(e["id2"] for e in ref["events"])
+    return {"workload": "1 star + 2 giants + 253 test particles, RKF78 1e-10, 1000 yr, ejection 15 AU, "
+                        "hit-centrum 1 AU (scenario file)",
+            "gpu": gpu, "cpu_port_1_core": cpu,
+            "reference_program": {k: ref[k] for k in ("accepted", "rejected", "evaluations", "wall_s",
+                                                      "energy_rel_drift", "machine")} | {"events": len(want)},
+            "ejected_in_common_with_reference": len(want & set(gpu["ejected_ids"])),
+            "speedup_vs_cpu_port": cpu["wall_s"] / gpu["wall_s"]}
+
+
+def _energies(integrals_bytes):
+    import struct
+    (ln,) = struct.unpack_from("<i", integrals_bytes, 0)
+    o, out = 4 + ln, []
+    while o < len(integrals_bytes):
+        (ne,) = struct.unpack_from("<i", integrals_bytes, o)
+        vals = struct.unpack_from(f"<{ne}d", integrals_bytes, o + 4)
+        out.append(vals[16])  # time, then the 16 values; the last is the total energy
+        o += 4 + 8 * ne
+    return out
+
+
 def small_systems_section(local):
-    """The latency-bound configurations: 256 bodies (1 star, 2 giants, 253 test
-    particles; adaptive RKF78 eps 1e-10) and 8,193 bodies with a gas nebula
-    (1 star, 2 giants, 8,190 planetesimals with drag; eps 1e-11), FP64, every
-    driver call of the sequence in one cooperative launch of the group driver
-    (k_group_rkf78: stage work spread over lanes and SM sub-partitions, the
-    few sources integrated by every CTA); the oracle on one core beside each."""
+    """The latency-bound configurations at their stated lengths: the 256-body
+    configuration (1 star, 2 giants, 253 test particles; adaptive RKF78 eps
+    1e-10) over its 1,000 years as a scenario run, and 8,193 bodies with a gas
+    nebula (1 star, 2 giants, 8,190 planetesimals with drag; eps 1e-11) for
+    10^4 accepted steps, FP64, every driver call of a sequence in one
+    cooperative launch of the group driver (k_group_rkf78); the oracle on one
+    core beside each."""
     import oracle
     from solaris_gb300 import abi, engine, scenarios
-    out = {}
-    for name, s, k, kc in (("config1_256_bodies", scenarios.config1(), 400, 100),
-                           ("config2_8193_bodies_gas", scenarios.config2(), 200, 20)):
-        with engine.Context(s, device=local) as ctx:
-            ctx.set_tolerance(s.epsilon)
-            ctx.set_state(s.y0)
-            tl = abi.SolTimeLine(0.0, s.h0, 0.0)
-            ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0, 0, 20, time_line=tl)
-            t0 = time.perf_counter()
-            r = ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0, 0, k, time_line=tl)
-            dt = time.perf_counter() - t0
-        acc, rej, evals = r["stats"]
-        o = oracle.Oracle(s)
-        o.set_eval_flags(abi.EVAL_ALL)
+    out = {"config1_256_bodies_1000yr": config1_full_run(local)}
+    s, k, kc = scenarios.config2(), 10000, 20
+    with engine.Context(s, device=local) as ctx:
+        ctx.set_tolerance(s.epsilon)
+        ctx.set_state(s.y0)
+        tl = abi.SolTimeLine(0.0, s.h0, 0.0)
         t0 = time.perf_counter()
-        ro = o.driver(abi.RUNGE_KUTTA_FEHLBERG78, s.y0, 0.0, s.h0, kc)
-        dtc = time.perf_counter() - t0
-        out[name] = {"steps_per_s": acc / dt, "evaluations_per_s": evals / dt,
-                     "pair_interactions_per_s": evals * s.pair_count() / dt,
-                     "body_evaluations_per_s": evals * s.n / dt, "accepted": acc, "rejected": rej,
-                     "cpu_port_1_core": {"steps_per_s": ro["stats"][0] / dtc,
-                                         "pair_interactions_per_s": ro["stats"][2] * s.pair_count() / dtc,
-                                         "kind": "port", "cores": 1, "sample": f"{kc} driver calls"}}
+        r = ctx.driver(abi.RUNGE_KUTTA_FEHLBERG78, 0, 0, k, time_line=tl)
+        dt = time.perf_counter() - t0
+    acc, rej, evals = r["stats"]
+    o = oracle.Oracle(s)
+    o.set_eval_flags(abi.EVAL_ALL)
+    t0 = time.perf_counter()
+    ro = o.driver(abi.RUNGE_KUTTA_FEHLBERG78, s.y0, 0.0, s.h0, kc)
+    dtc = time.perf_counter() - t0
+    out["config2_8193_bodies_gas_1e4_steps"] = {
+        "wall_s": dt, "steps_per_s": acc / dt, "evaluations_per_s": evals / dt,
+        "pair_interactions_per_s": evals * s.pair_count() / dt, "body_evaluations_per_s": evals * s.n / dt,
+        "accepted": acc, "rejected": rej, "simulated_days": tl.time,
+        "cpu_port_1_core": {"steps_per_s": ro["stats"][0] / dtc,
+                            "pair_interactions_per_s": ro["stats"][2] * s.pair_count() / dtc,
+                            "kind": "port", "cores": 1, "sample": f"the first {kc} driver calls"}}
     return out
 
 
