@@ -9,8 +9,10 @@ plus the Kepler terms, and the RK4 stage sums, all on the device.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  With N > 1 (torchrun) every rank integrates
-its own replica of the system (independent systems have no exchange step).
+Prints one JSON line (rank 0).  With N > 1 (torchrun, or started by this
+script itself) the system's sinks are partitioned over the GPUs, with one
+all-gather of positions per RK4 stage (strong scaling), and the ensemble's
+systems are split over them.
 """
 from __future__ import annotations
 
@@ -390,12 +392,112 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
+def relaunch_under_torchrun(args):
+    """`bench.py --gpus N` (N > 1) started as a plain process: run it again
+    as N ranks of torch.distributed.run on this node."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    os.execv(sys.executable, cmd)
+
+
+def run_sharded(args, rank, world, local):
+    """N > 1 GPUs: the one 65,536-body system with its sinks partitioned over
+    the ranks (solaris_gb300.sharded: per RK4 stage an all-gather of the
+    blocks' positions, each rank's pair kernels over its own sinks); total
+    work fixed, so the scaling is strong.  The ensemble's 4,096 systems are
+    split over the ranks (no exchange).  value = the system's pair
+    interactions per step / the slowest rank's time."""
+    import numpy as np
+    import torch
+
+    from solaris_gb300 import abi, build, engine, replicas, scenarios, sharded
+    build.build()
+    torch.cuda.set_device(local)
+    s = scenarios.config3(n=args.n)
+    pairs_step = 4 * s.pair_count()
+    sh = sharded.ShardedRK4(s, device=local, precision=abi.PRECISION_SPLIT_FF)
+    stream = sh.be.stream
+    l2_flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    sh.set_state(s.y0)
+    t = sh.step(0.0, s.h0, args.warmup)
+    sampler = ClockSampler(local)
+    replicas.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = engine.kernel_launches()
+    ms = 0.0
+    for _ in range(args.steps):
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        t = sh.step(t, s.h0, 1)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms += ev0.elapsed_time(ev1)
+    launches = engine.kernel_launches() - launches0
+    torch.cuda.synchronize()
+    replicas.barrier()
+    clocks = sampler.stop()
+    ms_step = replicas.max_over_ranks(ms / args.steps)
+    # end to end: the full state from pinned host memory in and back out every step
+    y_host = torch.empty(6 * s.n, dtype=torch.float64, pin_memory=True).numpy()
+    y_host[:] = sh.get_state()
+    ke = max(2, args.steps // 3)
+    replicas.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        sh.set_state(y_host)
+        t = sh.step(t, s.h0, 1)
+        y_host[:] = sh.get_state()
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0)
+    lo, hi = replicas.shard(4096, rank, world)
+    systems = scenarios.config4()[lo:hi]
+    with engine.Ensemble(systems, device=local, precision=abi.PRECISION_SPLIT_FF) as ens:
+        ens.set_state([x.y0 for x in systems], [0.0] * len(systems), [x.h0 for x in systems])
+        ens.autotune(steps=2)
+        ens.advance(2)
+        replicas.barrier()
+        t0 = time.perf_counter()
+        acc, _, _ = ens.advance(10)
+        dt = replicas.max_over_ranks(time.perf_counter() - t0)
+    ens_rate = replicas.sum_over_ranks(acc) / dt
+    sh.close()
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": pairs_step / (ms_step * 1e-3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "f64+f32 (split)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_bodies": s.n, "pairs_per_eval": s.pair_count(), "evals_per_step": 4,
+                       "integrator": "RungeKutta4", "precision": "split_ff",
+                       "l2": "flushed between timed steps (256 MiB write, outside the events)",
+                       "parallelism": f"sinks partitioned over {world} GPUs, positions all-gathered per stage"},
+            "e2e": {"value": pairs_step * ke / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * 6 * s.n,
+                    "d2h_bytes_per_step": 8 * 6 * s.n, "steps": ke,
+                    "api": "solaris_gb300.sharded.ShardedRK4 (host state in and out every step)"},
+            "gpu_launches": launches, "clocks": clocks,
+            "ensemble": {"value": ens_rate, "unit": "system-steps/s", "systems": 4096,
+                         "parallelism": f"systems split over {world} GPUs"}}))
+    replicas.finalize()
+
+
 def main():
     args = parse()
     from solaris_gb300 import replicas
+    world_env = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return relaunch_under_torchrun(args)
+    if world_env > 1 and world_env != args.gpus:
+        raise SystemExit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world_env}")
     rank, world, local = replicas.init()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if world > 1:
+        return run_sharded(args, rank, world, local)
 
     import numpy as np
     import torch
@@ -533,7 +635,7 @@ def main():
         "config": {"workload": WORKLOAD, "n_bodies": s.n, "pairs_per_eval": pairs_eval, "evals_per_step": 4,
                    "integrator": "RungeKutta4", "precision": head_name,
                    "l2": "flushed between timed steps (256 MiB write, outside the events)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "single GPU"},
         "forms": forms,
         "split_speedup_vs_fp64": value / forms["fp64"]["value"],
         "accuracy": {"bound": 1e-12, "reference_form": "fp64 (bit-identical to the reference CPU build)",

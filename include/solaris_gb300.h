@@ -207,6 +207,20 @@ int sol_accel_compute(sol_ctx* ctx, double t, const double* y, double* dydt,
                       double* rm3, int32_t* nn_idx, double* nn_dist);
 int sol_get_mig_type(const sol_ctx* ctx, int32_t* mig_type);
 
+/* Acceleration::Compute for the sinks [sink_begin, sink_end) only, on device
+ * buffers (a rank's block of a system whose sinks are partitioned over
+ * GPUs): d_y[6N] holds every body's state (every position is a source; a
+ * sink's own velocity is read), rows [sink_begin, sink_end) of d_dydt[6N]
+ * receive that sink's velocity and acceleration as Compute writes them, the
+ * other rows are untouched; rm3 and the nearest neighbours of those sinks
+ * are kept (sol_get_last_eval).  Enqueued on the context's stream
+ * (sol_get_stream) without waiting.  Heliocentric contexts; the context's
+ * precision and evaluate flags.  The reference evaluates every sink in one
+ * call (Solaris/Acceleration.cpp:248-329, the loop over i); the result rows
+ * are the same. */
+int sol_accel_sinks_device(sol_ctx* ctx, double t, const double* d_y, int32_t sink_begin, int32_t sink_end,
+                           double* d_dydt);
+
 /* ---- integrators: RungeKuttaFehlberg78::Driver, RungeKutta4::Driver,
  * DormandPrince::Driver (Solaris/RungeKuttaFehlberg78.h:22, RungeKutta4.h:15,
  * DormandPrince.h:14).  Each call performs n_steps driver calls on the

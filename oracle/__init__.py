@@ -21,6 +21,9 @@ LIB = os.path.join(BUILD_DIR, "liboracle.so")
 SRC = os.path.join(ORACLE_DIR, "solaris_oracle.c")
 REF_DIR = os.path.join(ORACLE_DIR, "_ref")
 REF_HARNESS = os.path.join(REF_DIR, "ref_harness")
+# Where the reference sources lie (read only by the build recipes and fixture
+# generators, never by the GPU tests or the bench).
+REFERENCE_SRC = os.environ.get("SOLARIS_REFERENCE_SRC", "/root/reference")
 
 
 def build(force: bool = False) -> str:
@@ -34,7 +37,7 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_reference(ref_root: str = "/root/reference") -> bool:
+def build_reference(ref_root: str = REFERENCE_SRC) -> bool:
     """Compile the reference CPU build into oracle/_ref (only where the
     reference sources exist)."""
     if not os.path.isdir(os.path.join(ref_root, "Solaris")):

@@ -241,6 +241,7 @@ def _declare(lib):
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
         "sol_gravity_noalloc_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
         "sol_set_wait_test": (C.c_int, [P, C.c_uint32, C.c_int32]),
+        "sol_accel_sinks_device": (C.c_int, [P, C.c_double, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -257,7 +258,7 @@ def exported_names():
         "sol_set_state", "sol_get_state", "sol_set_tolerance", "sol_set_device_loop", "sol_driver", "sol_driver_host",
         "sol_rkf78_step", "sol_get_last_eval", "sol_check_events", "sol_integrals", "sol_measure_fp64_peak",
         "sol_measure_fp64_pipe", "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc",
-        "sol_gravity_noalloc_status", "sol_set_wait_test",
+        "sol_gravity_noalloc_status", "sol_set_wait_test", "sol_accel_sinks_device",
         "sol_ensemble_create", "sol_ensemble_destroy", "sol_ensemble_set_precision", "sol_ensemble_set_tolerance",
         "sol_ensemble_set_state", "sol_ensemble_get_state", "sol_ensemble_advance", "sol_ensemble_configure",
         "sol_ensemble_autotune", "sol_adjoint_forward", "sol_adjoint_backward", "sol_set_masses",

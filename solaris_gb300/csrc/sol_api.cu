@@ -14,6 +14,8 @@ int sol_force_tile();
 int sol_force_part_doubles(int npad);
 int sol_force_uses_chunk_partials(const sol_ctx* c);
 int sol_force_prepass_blocks(int npad);
+int sol_force_src_doubles();
+int sol_force_launch_sinks(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int lo, int hi);
 int sol_integrate_partials_needed(int nv);
 int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_pe);
 
@@ -305,12 +307,12 @@ int sol_create(const sol_body_data* b, const sol_gas_component* gas, int32_t bar
       (rc = dev_alloc(&c->d_radius, N)) || (rc = dev_alloc(&c->d_density, N)) || (rc = dev_alloc(&c->d_cd, N)) ||
       (rc = dev_alloc(&c->d_gs, N)) || (rc = dev_alloc(&c->d_ge, N)) || (rc = dev_alloc(&c->d_rm3, N)) ||
       (rc = dev_alloc(&c->d_nn_dist, N)) || (rc = dev_alloc(&c->d_nn_idx, N)) ||
-      (rc = dev_alloc(&c->d_src, 8 * (size_t)c->npad)) ||
+      (rc = dev_alloc(&c->d_src, (size_t)sol_force_src_doubles() * c->npad)) ||
       (rc = dev_alloc(&c->d_drag, 3 * (size_t)(cl.n_spl + cl.n_pl))) ||
       (rc = dev_alloc(&c->d_mig1, 3 * (size_t)(cl.n_rocky + cl.n_proto))) ||
       (rc = dev_alloc(&c->d_mig2, 3 * (size_t)cl.n_giant)) ||
       (rc = dev_alloc(&c->d_ind_part, 6 * (size_t)sol_force_prepass_blocks(c->npad))) ||
-      (rc = dev_alloc(&c->d_ind_sum, 6)) || (rc = dev_alloc(&c->d_y0, NV)) || (rc = dev_alloc(&c->d_y, NV)) ||
+      (rc = dev_alloc(&c->d_ind_sum, 8)) || (rc = dev_alloc(&c->d_y0, NV)) || (rc = dev_alloc(&c->d_y, NV)) ||
       (rc = dev_alloc(&c->d_accel, NV)) || (rc = dev_alloc(&c->d_yscale, NV)) || (rc = dev_alloc(&c->d_err, NV)) ||
       (rc = dev_alloc(&c->d_ytmp, NV)) || (rc = dev_alloc(&c->d_io_in, NV)) || (rc = dev_alloc(&c->d_io_out, NV)))
     return fail(rc);
@@ -923,6 +925,24 @@ int sol_bench_force(sol_ctx* c, int32_t precision, int32_t reps, double* ms_per_
 int sol_measure_fp64_peak(int32_t device, double* flops) {
   if (!flops) return SOL_ERR_ARG;
   return sol_fp64_peak_launch(device, flops);
+}
+
+int sol_accel_sinks_device(sol_ctx* c, double t, const double* d_y, int32_t sink_begin, int32_t sink_end,
+                           double* d_dydt) {
+  RET(check_ctx(c));
+  if (!d_y || !d_dydt || sink_begin < 0 || sink_end < sink_begin || sink_end > c->n) {
+    sol_set_error("sol_accel_sinks_device: bad arguments (sinks [%d, %d) of %d bodies)", sink_begin, sink_end, c->n);
+    return SOL_ERR_ARG;
+  }
+  if (c->barycentric) {
+    sol_set_error("sol_accel_sinks_device: heliocentric contexts only");
+    return SOL_ERR_ARG;
+  }
+  RET(set_device(c));
+  TimeSpec ts{nullptr, nullptr, 0.0, t};
+  RET(sol_force_launch_sinks(c, d_y, d_dydt, ts, c->eval_flags, sink_begin, sink_end));
+  c->last_eval_valid = 1;
+  return SOL_OK;
 }
 
 int sol_set_wait_test(sol_ctx* c, uint32_t spin_limit, int32_t withhold) {

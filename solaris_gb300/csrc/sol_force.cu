@@ -19,6 +19,9 @@
 
 #include "sol_internal.cuh"
 #include "sol_crmath.cuh"
+#include "sol_pair.cuh"
+
+int sol_force_uses_chunk_partials(const sol_ctx* c);
 
 namespace {
 
@@ -27,6 +30,14 @@ constexpr int kTile = 256;       // sources per shared-memory tile
 constexpr int kPrepassBlock = 256;
 
 enum SrcArray { SX = 0, SY, SZ, SGM, SPX, SPY, SPZ, SGF, SRC_ARRAYS = 8 };  // SGF: G m as (hi, lo) floats
+// Float table of the SPLIT_FF 2-D kernel, after the SRC_ARRAYS doubles: each
+// coordinate as its grid triple a + b + c (f2_grid_disp in sol_pair.cuh) and
+// G m as (hi, lo), one float array each (two sources load as one float2).
+enum FTab { FAX = 0, FBX, FCX, FAY, FBY, FCY, FAZ, FBZ, FCZ, FGH, FGL, FTAB_USED = 11, FTAB_ARRAYS = 12 };
+constexpr int kSrcDoubles = SRC_ARRAYS + FTAB_ARRAYS / 2;  // doubles per padded body in the source table
+// ind_sum slots: [0..5] the indirect sums, [6] the grid G1 of the float table,
+// [7] (low word) the running maximum |coordinate| as FP32 bits (atomicMax)
+constexpr int kIndGrid = 6, kIndMaxWord = 7;
 
 constexpr int kChunkTiles = 16;             // sources per work unit of the 2-D pair kernel
 constexpr int kChunk = kChunkTiles * kTile;  // 4,096
@@ -37,10 +48,16 @@ __device__ __forceinline__ double eval_time(const TimeSpec& ts) {
 }
 
 // ---- prepass ----------------------------------------------------------------
-__global__ void k_prepass(ForceCtx fc, const double* __restrict__ y, int split) {
+__device__ __forceinline__ float* ftab(const ForceCtx& fc) { return reinterpret_cast<float*>(fc.src + (size_t)SRC_ARRAYS * fc.npad); }
+
+// prec: SOL_PRECISION_*.  The split forms also sum the indirect term; SPLIT_FF
+// (2-D kernel, ff = 1) also takes the largest |coordinate| and writes G m as
+// float (hi, lo) arrays of the float table.
+__global__ void k_prepass(ForceCtx fc, const double* __restrict__ y, int split, int ff) {
   const int n = fc.cls.n;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   double q[6] = {0, 0, 0, 0, 0, 0};  // indirect contributions: massive range, super-planetesimal range
+  unsigned mbits = 0;                 // |coordinate| maximum as FP32 bits, rounded up
   if (j < fc.npad) {
     double x = 0, yy = 0, z = 0, gm = 0, px = 0, py = 0, pz = 0;
     if (j < n) {
@@ -83,6 +100,17 @@ __global__ void k_prepass(ForceCtx fc, const double* __restrict__ y, int split) 
     float gh = __double2float_rn(gm);
     float gl = __double2float_rn(gm - (double)gh);
     reinterpret_cast<float2*>(s + (size_t)SGF * np)[j] = make_float2(gh, gl);
+    if (ff) {
+      float* T = ftab(fc);
+      T[(size_t)FGH * np + j] = gh;
+      T[(size_t)FGL * np + j] = gl;
+      const double m = fmax(fabs(x), fmax(fabs(yy), fabs(z)));
+      mbits = __float_as_uint(__double2float_ru(m));
+    }
+  }
+  if (ff) {
+    const unsigned wmax = __reduce_max_sync(0xFFFFFFFFu, mbits);
+    if ((threadIdx.x & 31) == 0 && wmax) atomicMax(reinterpret_cast<unsigned*>(fc.ind_sum + kIndMaxWord), wmax);
   }
   if (!split) return;
   // fixed-order block tree reduction of the indirect contributions
@@ -117,6 +145,37 @@ __global__ void k_ind_reduce(ForceCtx fc) {
       fc.ind_sum[k] = red[k][0];
       fc.ind_sum[3 + k] = red[k][0] + red[3 + k][0];
     }
+    // the float table's grid: G1 = 2^(E - 23) with every |coordinate| < 2^E
+    // (then read and cleared for the next evaluation's maximum)
+    unsigned* word = reinterpret_cast<unsigned*>(fc.ind_sum + kIndMaxWord);
+    const unsigned mb = *word;
+    const int E = mb ? (int)((mb >> 23) & 0xFFu) - 127 + 1 : 0;
+    fc.ind_sum[kIndGrid] = ldexp(1.0, max(E, -90) - 23);
+    *word = 0u;
+  }
+}
+
+// Grid triples of every coordinate (f2_grid_disp): a = G1 rint(x / G1),
+// b = G2 rint((x - a) / G2), c = float(x - a - b); a and b are exact floats
+// (at most 2^23 of their grid), x - a and x - a - b exact doubles.  Padding
+// bodies get zeros.
+__global__ void k_split_table(ForceCtx fc, const double* __restrict__ y) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= fc.npad) return;
+  const double G1 = fc.ind_sum[kIndGrid];
+  const double G2 = G1 * 0x1.0p-24;
+  const double iG1 = 1.0 / G1, iG2 = 1.0 / G2;  // powers of two: exact
+  float* T = ftab(fc);
+  const int np = fc.npad;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double x = j < fc.cls.n ? y[6 * j + k] : 0.0;
+    const double a = rint(x * iG1) * G1;
+    const double r = x - a;
+    const double b = rint(r * iG2) * G2;
+    T[(size_t)(FAX + 3 * k) * np + j] = (float)a;
+    T[(size_t)(FBX + 3 * k) * np + j] = (float)b;
+    T[(size_t)(FCX + 3 * k) * np + j] = __double2float_rn(r - b);
   }
 }
 
@@ -212,9 +271,9 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_ac(ForceCtx fc, const do
   constexpr int NARR = (PREC == SOL_PRECISION_FP64) ? 7 : 4;
   __shared__ __align__(128) TileSmem<NARR> sm;
   const Classes& c = fc.cls;
-  const int n = c.n;
-  const int i = blockIdx.x * kSinkBlock + threadIdx.x;
-  const int i_first = blockIdx.x * kSinkBlock;
+  const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
+  const int i = fc.sink_lo + blockIdx.x * kSinkBlock + threadIdx.x;
+  const int i_first = fc.sink_lo + blockIdx.x * kSinkBlock;
   // NOfMassive of GravityAC (:285-289); types are sorted, so the first sink
   // of the CTA has the largest source range.
   const int ns_cta = (fc.type[min(i_first, n - 1)] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
@@ -375,8 +434,8 @@ __global__ void __launch_bounds__(256) k_gravity_ac_few(ForceCtx fc, const doubl
   __shared__ int sink_ns[kFewSinks];
   __shared__ double acc[kFewTerms];
   const Classes& c = fc.cls;
-  const int n = c.n;
-  const int i0 = blockIdx.x * kFewSinks;
+  const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
+  const int i0 = fc.sink_lo + blockIdx.x * kFewSinks;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x < kFewSinks) {
     const int i = i0 + threadIdx.x;
@@ -590,8 +649,8 @@ __global__ void __launch_bounds__(kWideWarps * 32, kWideCtasPerSm) k_gravity_ac_
   __shared__ unsigned long long nn_key[kWideWarps][kWideSinks];
   __shared__ int nn_j[kWideWarps][kWideSinks];
   const Classes& c = fc.cls;
-  const int n = c.n;
-  const int i0 = blockIdx.x * spc;
+  const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
+  const int i0 = fc.sink_lo + blockIdx.x * spc;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x < kWideSinks) {
     const int i = i0 + threadIdx.x;
@@ -777,10 +836,10 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
   constexpr int NARR = 4;  // x, y, z and G m (FP64 for SPLIT, float-float for SPLIT_FF)
   __shared__ __align__(128) TileSmem<NARR> sm;
   const Classes& c = fc.cls;
-  const int n = c.n;
+  const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
   const int np = fc.npad;
-  const int i = blockIdx.x * kSinkBlock + threadIdx.x;
-  const int i_first = blockIdx.x * kSinkBlock;
+  const int i = fc.sink_lo + blockIdx.x * kSinkBlock + threadIdx.x;
+  const int i_first = fc.sink_lo + blockIdx.x * kSinkBlock;
   const int ns_cta = (fc.type[min(i_first, n - 1)] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
   const int ns = (i < n && fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
   const int j_begin = blockIdx.y * kChunk;
@@ -879,6 +938,207 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
   part[base + PIDX * np] = __longlong_as_double((long long)nn);
 }
 
+// ---- SPLIT_FF 2-D kernel: float-float pairs with no FP64 instruction -------
+// Same grid as k_pairs (blockIdx.x: kSinkBlock sinks; blockIdx.y: a chunk of
+// kChunk sources) and the same partial outputs for k_combine.  The sources'
+// grid triples and G m (hi, lo) arrive tile by tile in shared memory by bulk
+// copies; each thread takes two sources per step in paired FP32
+// instructions: the displacement from the grid triples (exact parts, no
+// FP64), r^2, G m r^-3 and the accumulation in float-float (sol_pair.cuh).
+// Pairs closer than the grid G1 (|d| < G1, where the triple displacement
+// would lose relative accuracy) take FP64 arithmetic, as pairs below 1e-12 AU
+// do in the other float-float kernels.  Tiles whose sources are all valid
+// for every sink of the warp (no sink index, no central body, no source
+// beyond a sink's source count or the chunk) run without per-pair tests.
+constexpr int kFF = FTAB_USED;
+
+struct FFTile {
+  float v[2][kFF][kTile];
+  uint64_t bar[2];
+};
+
+// One FP64 pair of the close-pair branch: G m r^-3 d into (fx, fy, fz);
+// r^2 for the nearest-neighbour comparison as (hi, lo) floats.
+__device__ __forceinline__ void ff_close_pair(const ForceCtx& fc, int j, double xi, double yi, double zi, float gh,
+                                           float gl, double& fx, double& fy, double& fz, float& r2h, float& r2l) {
+  const double* s = fc.src;
+  const int np = fc.npad;
+  const double dx = s[SX * np + j] - xi, dy = s[SY * np + j] - yi, dz = s[SZ * np + j] - zi;
+  const double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, dz * dz));
+  r2h = __double2float_rn(r2);
+  r2l = __double2float_rn(r2 - (double)r2h);
+  if (r2 > 0.0) {
+    const double rinv = __drcp_rn(__dsqrt_rn(r2));
+    const double sd = ((double)gh + (double)gl) * (rinv * rinv * rinv);
+    fx = __fma_rn(sd, dx, fx);
+    fy = __fma_rn(sd, dy, fy);
+    fz = __fma_rn(sd, dz, fz);
+  }
+}
+
+// Nearest-neighbour candidate: the smallest r^2 (hi, then lo), the first in
+// ascending source order.
+__device__ __forceinline__ void ff_nn(float r2h, float r2l, bool ok, int j, float& mh, float& ml, int& nn) {
+  const bool better = ok & ((r2h < mh) | ((r2h == mh) & (r2l < ml)));
+  mh = better ? r2h : mh;
+  ml = better ? r2l : ml;
+  nn = better ? j : nn;
+}
+
+// Two sources (j, j + 1) of the tile against the sink.  MASKED: per-pair
+// validity (source range, the sink itself, the chunk end) is tested.
+template <bool MASKED>
+__device__ __forceinline__ void ff_two_sources(const FFTile& sm, int st, int jj, int j, int i, int ns, int jend,
+                                               const float* ai, const float* bi, const float* ci, float thr,
+                                               const ForceCtx& fc, double xi, double yi, double zi, float2* Ah,
+                                               float2* Al, double& fx, double& fy, double& fz, float& mh, float& ml,
+                                               int& nn) {
+  float2 h[3], l[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    f2_grid_disp(*reinterpret_cast<const float2*>(&sm.v[st][FAX + 3 * k][jj]),
+                 *reinterpret_cast<const float2*>(&sm.v[st][FBX + 3 * k][jj]),
+                 *reinterpret_cast<const float2*>(&sm.v[st][FCX + 3 * k][jj]), ai[k], bi[k], ci[k], h[k], l[k]);
+  float2 gh = *reinterpret_cast<const float2*>(&sm.v[st][FGH][jj]);
+  float2 gl = *reinterpret_cast<const float2*>(&sm.v[st][FGL][jj]);
+  float2 r2h, r2l;
+  f2_ff_r2(h, l, r2h, r2l);
+  bool ok0 = true, ok1 = true;
+  if constexpr (MASKED) {
+    ok0 = (j >= 1) & (j < ns) & (j != i) & (j < jend);
+    ok1 = (j + 1 >= 1) & (j + 1 < ns) & (j + 1 != i) & (j + 1 < jend);
+  }
+  float2 qh = r2h, ql = r2l;
+  if (!ok0 || r2h.x < thr) {
+    if (ok0) ff_close_pair(fc, j, xi, yi, zi, gh.x, gl.x, fx, fy, fz, r2h.x, r2l.x);
+    gh.x = gl.x = 0.0f;
+    qh.x = 1.0f;
+    ql.x = 0.0f;
+  }
+  if (!ok1 || r2h.y < thr) {
+    if (ok1) ff_close_pair(fc, j + 1, xi, yi, zi, gh.y, gl.y, fx, fy, fz, r2h.y, r2l.y);
+    gh.y = gl.y = 0.0f;
+    qh.y = 1.0f;
+    ql.y = 0.0f;
+  }
+  float2 sh, se;
+  f2_ff_gm_rinv3(qh, ql, gh, gl, sh, se);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) f2_ff_accumulate(Ah[k], Al[k], sh, se, h[k], l[k]);
+  ff_nn(r2h.x, r2l.x, ok0, j, mh, ml, nn);
+  ff_nn(r2h.y, r2l.y, ok1, j + 1, mh, ml, nn);
+}
+
+__global__ void __launch_bounds__(kSinkBlock) k_pairs_ff(ForceCtx fc, const double* __restrict__ y,
+                                                         double* __restrict__ part, int* dev_status) {
+  __shared__ __align__(128) FFTile sm;
+  const Classes& c = fc.cls;
+  const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
+  const int np = fc.npad;
+  const int i = fc.sink_lo + blockIdx.x * kSinkBlock + threadIdx.x;
+  const int i_first = fc.sink_lo + blockIdx.x * kSinkBlock;
+  const int ns_cta = (fc.type[min(i_first, n - 1)] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
+  const int ns = (i < n && fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
+  const int j_begin = blockIdx.y * kChunk;
+  const int j_end = min(j_begin + kChunk, ns_cta);
+  const int t_begin = j_begin / kTile;
+  const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
+  const bool live = i < n && i >= 1;
+
+  const float* T = ftab(fc);
+  float ai[3], bi[3], ci[3];
+  double xi = 0, yi = 0, zi = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    ai[k] = i < n ? T[(size_t)(FAX + 3 * k) * np + i] : 0.0f;
+    bi[k] = i < n ? T[(size_t)(FBX + 3 * k) * np + i] : 0.0f;
+    ci[k] = i < n ? T[(size_t)(FCX + 3 * k) * np + i] : 0.0f;
+  }
+  if (i < n) {
+    xi = y[6 * i + 0];
+    yi = y[6 * i + 1];
+    zi = y[6 * i + 2];
+  }
+  const double G1 = fc.ind_sum[kIndGrid];
+  const float thr = (float)(G1 * G1);  // |d| < G1: the FP64 branch
+
+  if (threadIdx.x == 0) {
+    sol_mbar_init(&sm.bar[0], 1);
+    sol_mbar_init(&sm.bar[1], 1);
+    sol_fence_barrier_init();
+  }
+  __syncthreads();
+  auto issue = [&](int t, int stage) {
+    sol_mbar_expect_tx(&sm.bar[stage], kFF * kTile * 4);
+    for (int k = 0; k < kFF; ++k)
+      sol_bulk_g2s(&sm.v[stage][k][0], T + (size_t)k * np + (size_t)(t_begin + t) * kTile, kTile * 4,
+                   &sm.bar[stage]);
+  };
+  if (threadIdx.x == 0) {
+    if (ntiles > 0) issue(0, 0);
+    if (ntiles > 1) issue(1, 1);
+  }
+  double ax = 0.0, ay = 0.0, az = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;  // chunk sums, compensated
+  double fx = 0.0, fy = 0.0, fz = 0.0;                                  // close pairs, FP64
+  float mh = 3.0e38f, ml = 0.0f;
+  int nn = -1;
+  int issued = ntiles < 2 ? ntiles : 2;
+  int t = 0;
+  bool timed_out = false;
+  for (; t < ntiles; ++t) {
+    const int st = t & 1;
+    const bool ok = sol_mbar_wait(&sm.bar[st], (t >> 1) & 1);
+    const int j0 = (t_begin + t) * kTile;
+    const int jend = min(j0 + kTile, j_end);
+    // the warp's sinks all see every source of the tile, none of them is in it
+    const bool clean = live && j0 >= 1 && jend == j0 + kTile && j0 + kTile <= ns && (i < j0 || i >= j0 + kTile);
+    const bool fast = __all_sync(0xFFFFFFFFu, clean);
+    if (ok && live) {
+      float2 Ah[3], Al[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) Ah[k] = Al[k] = make_float2(0.0f, 0.0f);
+      if (fast) {
+#pragma unroll 2
+        for (int jj = 0; jj < kTile; jj += 2)
+          ff_two_sources<false>(sm, st, jj, j0 + jj, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy,
+                                fz, mh, ml, nn);
+      } else {
+        for (int jj = 0; jj < jend - j0; jj += 2)
+          ff_two_sources<true>(sm, st, jj, j0 + jj, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy,
+                               fz, mh, ml, nn);
+      }
+      // the tile's float-float partials (even and odd sources) into the FP64 chunk sums
+      two_sum(ax, cx, ((double)Ah[0].x + (double)Al[0].x) + ((double)Ah[0].y + (double)Al[0].y));
+      two_sum(ay, cy, ((double)Ah[1].x + (double)Al[1].x) + ((double)Ah[1].y + (double)Al[1].y));
+      two_sum(az, cz, ((double)Ah[2].x + (double)Al[2].x) + ((double)Ah[2].y + (double)Al[2].y));
+    }
+    if (__syncthreads_or(!ok)) {
+      timed_out = true;
+      break;
+    }
+    if (threadIdx.x == 0 && t + 2 < ntiles) {
+      sol_fence_proxy_async();
+      issue(t + 2, st);
+    }
+    if (t + 2 < ntiles) issued = t + 3;
+  }
+  if (timed_out) {
+    if (threadIdx.x == 0) {
+      atomicOr(dev_status, SOL_DEV_TIMEOUT);
+      for (int u = t; u < issued; ++u) sol_mbar_wait(&sm.bar[u & 1], (u >> 1) & 1);
+    }
+    __syncthreads();
+    return;
+  }
+  if (i >= n) return;
+  const size_t base = (size_t)blockIdx.y * PART_SLOTS * np + i;
+  part[base + PAX * np] = (ax + cx) + fx;
+  part[base + PAY * np] = (ay + cy) + fy;
+  part[base + PAZ * np] = (az + cz) + fz;
+  part[base + PR2 * np] = nn >= 0 ? (double)mh + (double)ml : 1.0e300;
+  part[base + PIDX * np] = __longlong_as_double((long long)nn);
+}
+
 // Per sink: the chunk partials in chunk order, the nearest neighbour (the
 // smallest r^2, ties to the lower index as the reference's ascending scan),
 // distanceOfNN recomputed in the reference's FP64 arithmetic for the chosen
@@ -886,9 +1146,9 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
 __global__ void k_combine(ForceCtx fc, const double* __restrict__ y, double* __restrict__ dydt,
                           const double* __restrict__ part, int nchunk, TimeSpec ts, uint32_t flags) {
   const Classes& c = fc.cls;
-  const int n = c.n;
+  const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
   const int np = fc.npad;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = fc.sink_lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double* out = dydt + 6 * i;
   if (i == 0) {
@@ -986,10 +1246,10 @@ __global__ void __launch_bounds__(kFewSplitWarps * 32) k_pairs_few(ForceCtx fc, 
                                                                    double* __restrict__ dydt, TimeSpec ts,
                                                                    uint32_t flags) {
   const Classes& c = fc.cls;
-  const int n = c.n;
+  const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
   const int np = fc.npad;
   const int lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kFewSplitWarps + (threadIdx.x >> 5);
+  const int i = fc.sink_lo + blockIdx.x * kFewSplitWarps + (threadIdx.x >> 5);
   if (i >= n) return;  // whole warps leave together
   const int ns = (i >= 1) ? ((fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm) : 0;
   const double xi = y[6 * i + 0], yi = y[6 * i + 1], zi = y[6 * i + 2];
@@ -1119,20 +1379,29 @@ __global__ void __launch_bounds__(kFewSplitWarps * 32) k_pairs_few(ForceCtx fc, 
 }  // namespace
 
 // parts: 1 = prepass (and indirect totals), 2 = pair kernel, 3 = both.
-int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int parts) {
-  ForceCtx& fc = c->fc;
+// The sinks of fc's range [sink_lo, sol_sink_hi) (every body by default);
+// the prepass always covers every body (the sources).
+static int force_launch(sol_ctx* c, const ForceCtx& fc, const double* d_y, double* d_dydt, TimeSpec ts,
+                        uint32_t flags, int parts) {
+  const int nsink = sol_sink_hi(fc) - fc.sink_lo;
   const int split = (c->precision != SOL_PRECISION_FP64 && !c->barycentric) ? 1 : 0;
+  // SPLIT_FF systems beyond the warp-per-sink kernel run k_pairs_ff on the float table
+  const int ff2d = split && c->precision == SOL_PRECISION_SPLIT_FF && sol_force_uses_chunk_partials(c);
   if (parts & 1) {
     const int nb_pre = (fc.npad + kPrepassBlock - 1) / kPrepassBlock;
-    k_prepass<<<nb_pre, kPrepassBlock, 0, c->stream>>>(fc, d_y, split);
+    k_prepass<<<nb_pre, kPrepassBlock, 0, c->stream>>>(fc, d_y, split, ff2d);
     SOL_LAUNCHED();
     if (split && !c->barycentric) {
       k_ind_reduce<<<1, 256, 0, c->stream>>>(fc);
       SOL_LAUNCHED();
     }
+    if (ff2d) {
+      k_split_table<<<nb_pre, kPrepassBlock, 0, c->stream>>>(fc, d_y);
+      SOL_LAUNCHED();
+    }
   }
-  if (!(parts & 2)) return SOL_OK;
-  const int nb = (c->n + kSinkBlock - 1) / kSinkBlock;
+  if (!(parts & 2) || nsink <= 0) return SOL_OK;
+  const int nb = (nsink + kSinkBlock - 1) / kSinkBlock;
   if (c->barycentric) {
     k_gravity_bc<<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
     SOL_LAUNCHED();
@@ -1155,10 +1424,10 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
     const int slots = kWideCtasPerSm * wide_sms[dev];
     int spc = 0;
     {
-      const int k0 = (c->n + slots * kWideSinks - 1) / (slots * kWideSinks);
+      const int k0 = (nsink + slots * kWideSinks - 1) / (slots * kWideSinks);
       double best = 1e300;
       for (int k = k0; k < k0 + 3; ++k) {
-        const int sp = (c->n + k * slots - 1) / (k * slots);
+        const int sp = (nsink + k * slots - 1) / (k * slots);
         const double cost = k * (0.4375 * sp + 3.0);
         if (cost < best) {
           best = cost;
@@ -1167,16 +1436,16 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
       }
     }
     if (spc >= kWideMinSinks) {
-      k_gravity_ac_wide<<<(c->n + spc - 1) / spc, kWideWarps * 32, kWideSmem, c->stream>>>(fc, d_y, d_dydt, ts,
-                                                                                           flags, spc);
+      k_gravity_ac_wide<<<(nsink + spc - 1) / spc, kWideWarps * 32, kWideSmem, c->stream>>>(fc, d_y, d_dydt, ts,
+                                                                                            flags, spc);
     } else {
-      k_gravity_ac_few<<<(c->n + kFewSinks - 1) / kFewSinks, 256, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
+      k_gravity_ac_few<<<(nsink + kFewSinks - 1) / kFewSinks, 256, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
     }
     SOL_LAUNCHED();
     return SOL_OK;
   }
   if (split && c->n <= kFewSplitMax && c->cls.nm + c->cls.n_spl >= kTile) {
-    const int grid = (c->n + kFewSplitWarps - 1) / kFewSplitWarps;
+    const int grid = (nsink + kFewSplitWarps - 1) / kFewSplitWarps;
     if (c->precision == SOL_PRECISION_SPLIT_FF)
       k_pairs_few<SOL_PRECISION_SPLIT_FF><<<grid, kFewSplitWarps * 32, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
     else
@@ -1192,11 +1461,11 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
     const int nchunk = (c->n + kChunk - 1) / kChunk;
     dim3 grid(nb, nchunk);
     if (c->precision == SOL_PRECISION_SPLIT_FF)
-      k_pairs<SOL_PRECISION_SPLIT_FF><<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status);
+      k_pairs_ff<<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status);
     else
       k_pairs<SOL_PRECISION_SPLIT><<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status);
     SOL_LAUNCHED();
-    k_combine<<<(c->n + 255) / 256, 256, 0, c->stream>>>(fc, d_y, d_dydt, c->d_part, nchunk, ts, flags);
+    k_combine<<<(nsink + 255) / 256, 256, 0, c->stream>>>(fc, d_y, d_dydt, c->d_part, nchunk, ts, flags);
   } else {
     k_gravity_ac<SOL_PRECISION_FP64><<<nb, kSinkBlock, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags,
                                                                        &c->d_ctrl->dev_status, SOL_SPIN_LIMIT, -1);
@@ -1205,11 +1474,26 @@ int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
   return SOL_OK;
 }
 
+int sol_force_launch_parts(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int parts) {
+  return force_launch(c, c->fc, d_y, d_dydt, ts, flags, parts);
+}
+
 int sol_force_launch(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags) {
   return sol_force_launch_parts(c, d_y, d_dydt, ts, flags, 3);
 }
 
+// Sinks [lo, hi) only (heliocentric contexts): a rank's block of a
+// sink-partitioned system.
+int sol_force_launch_sinks(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int lo,
+                           int hi) {
+  ForceCtx fc = c->fc;
+  fc.sink_lo = lo;
+  fc.sink_hi = hi;
+  return force_launch(c, fc, d_y, d_dydt, ts, flags, 3);
+}
+
 int sol_force_tile() { return kTile; }
+int sol_force_src_doubles() { return kSrcDoubles; }
 int sol_force_part_doubles(int npad) { return ((npad + kChunk - 1) / kChunk) * PART_SLOTS * npad; }
 // whether the split forms of this system run the 2-D kernel (and need its
 // chunk partials); the same test as the dispatch in sol_force_launch_parts
@@ -1362,7 +1646,7 @@ extern "C" int sol_gravity_noalloc(const sol_nbodies* counts, const int32_t* d_t
   // reference, whose rm3 array starts zeroed (Acceleration.cpp:65-69).
   SOL_CUDA(cudaMemsetAsync(d_rm3, 0, sizeof(double), st));
   const int split = precision == SOL_PRECISION_SPLIT;
-  k_prepass<<<fc.n_ind_blocks, kPrepassBlock, 0, st>>>(fc, d_y, split);
+  k_prepass<<<fc.n_ind_blocks, kPrepassBlock, 0, st>>>(fc, d_y, split, 0);
   SOL_LAUNCHED();
   if (split) {
     k_ind_reduce<<<1, 256, 0, st>>>(fc);

@@ -116,7 +116,11 @@ struct ForceCtx {
   double* ind_sum;     // [6]: indirect sums over [1, nm) and [1, nm + spl)
   int n_ind_blocks;
   int has_mig1, has_mig2;
+  // sinks evaluated: [sink_lo, sink_hi); sink_hi == 0 means every body (a
+  // rank of a sink-partitioned system evaluates its own block)
+  int sink_lo, sink_hi;
 };
+__host__ __device__ __forceinline__ int sol_sink_hi(const ForceCtx& fc) { return fc.sink_hi ? fc.sink_hi : fc.cls.n; }
 
 // A captured driver call (RKF78 or DP) with its device-side attempt loop.
 struct DriverGraph {

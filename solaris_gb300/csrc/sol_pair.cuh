@@ -107,3 +107,103 @@ __device__ __forceinline__ void ff_pair_accumulate(double dxd, double dyd, doubl
   r2h_out = r2h;
   r2l_out = r2l;
 }
+
+// ---- paired FP32 (f32x2): one instruction computes two lanes ----------------
+// Blackwell's paired FP32 arithmetic (add / sub / mul / fma .f32x2, round to
+// nearest even per lane) halves the instruction count of float-float code
+// that processes two sources at once.
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;"
+      : "=l"(r)
+      : "l"(*reinterpret_cast<const unsigned long long*>(&a)), "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+  return *reinterpret_cast<const float2*>(&r);
+}
+__device__ __forceinline__ float2 f2_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 f2_splat(float v) { return make_float2(v, v); }
+// TwoSum (Knuth), FastTwoSum (Dekker, |a| >= |b| or a == 0), TwoProduct by FMA
+__device__ __forceinline__ void f2_two_sum(float2 a, float2 b, float2& s, float2& e) {
+  s = f2_add(a, b);
+  const float2 bb = f2_sub(s, a);
+  e = f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb));
+}
+__device__ __forceinline__ void f2_fast_two_sum(float2 a, float2 b, float2& s, float2& e) {
+  s = f2_add(a, b);
+  e = f2_sub(b, f2_sub(s, a));
+}
+__device__ __forceinline__ void f2_two_prod(float2 a, float2 b, float2& p, float2& e) {
+  p = f2_mul(a, b);
+  e = f2_fma(a, b, f2_neg(p));
+}
+
+// ---- displacement from grid triples (the SPLIT_FF 2-D kernel) ----------------
+// Every coordinate is stored as x = a + b + c: a a multiple of the grid G1
+// (|a| <= 2^23 G1), b a multiple of G2 = G1 2^-24 (|b| <= G1 / 2), c the
+// float nearest the rest (|c| <= G2 / 2), G1 a power of two with every |x|
+// below 2^23 G1.  Then a_j - a_i and b_j - b_i are exact in FP32 (multiples
+// of one grid, at most 2^24 of it), and
+//   d = (a_j - a_i) + (b_j - b_i) + (c_j - c_i)
+// is formed as a float-float (h, l) with an absolute error below ~2^-22 G2,
+// i.e. 2^-46 |d| for |d| >= G1 / 2: the FastTwoSum of the two exact parts
+// (|a_j - a_i| >= G1 >= |b_j - b_i| unless a_j = a_i), the rounded c part
+// added to the low word, one more FastTwoSum.  No FP64 instruction.
+__device__ __forceinline__ void f2_grid_disp(float2 aj, float2 bj, float2 cj, float ai, float bi, float ci, float2& h,
+                                             float2& l) {
+  const float2 s1 = f2_sub(aj, f2_splat(ai));
+  const float2 s2 = f2_sub(bj, f2_splat(bi));
+  const float2 s3 = f2_sub(cj, f2_splat(ci));
+  float2 hh, l0;
+  f2_fast_two_sum(s1, s2, hh, l0);
+  f2_fast_two_sum(hh, f2_add(l0, s3), h, l);
+}
+
+// r^2 = sum_k (h_k + l_k)^2 as a float-float (exact squares of the high
+// words, TwoSum of the three non-negative squares, the cross terms 2 h l
+// and the squares' errors in the low word).
+__device__ __forceinline__ void f2_ff_r2(const float2* h, const float2* l, float2& r2h, float2& r2l) {
+  float2 p[3], e[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) f2_two_prod(h[k], h[k], p[k], e[k]);
+  float2 s12, t12, s3, t3;
+  f2_two_sum(p[0], p[1], s12, t12);
+  f2_two_sum(s12, p[2], s3, t3);
+  float2 lo = f2_add(f2_add(t12, t3), f2_add(f2_add(e[0], e[1]), e[2]));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) lo = f2_fma(f2_add(h[k], h[k]), l[k], lo);
+  f2_fast_two_sum(s3, lo, r2h, r2l);
+}
+
+// G m r^-3 as a float-float from r^2 = (qh, ql): the FP32 rsqrt seed y, the
+// residual e = 1 - r^2 y^2 from exact products, r^-3 = y^3 (1 + 3/2 e +
+// 15/8 e^2) (|e| < 2^-21: truncation ~2^-60), times G m = (gh, gl).
+__device__ __forceinline__ void f2_ff_gm_rinv3(float2 qh, float2 ql, float2 gh, float2 gl, float2& sh, float2& se) {
+  const float2 y = make_float2(rsqrtf(qh.x), rsqrtf(qh.y));
+  float2 y2, y2e, q, qe;
+  f2_two_prod(y, y, y2, y2e);
+  f2_two_prod(qh, y2, q, qe);
+  const float2 e = f2_sub(f2_sub(f2_sub(f2_splat(1.0f), q), qe), f2_fma(qh, y2e, f2_mul(ql, y2)));
+  float2 y3h, y3e;
+  f2_two_prod(y2, y, y3h, y3e);
+  y3e = f2_fma(y2e, y, y3e);
+  const float2 c = f2_mul(e, f2_fma(f2_splat(1.875f), e, f2_splat(1.5f)));
+  float2 Rh, Rl;
+  f2_fast_two_sum(y3h, f2_fma(y3h, c, y3e), Rh, Rl);
+  f2_two_prod(gh, Rh, sh, se);
+  se = f2_fma(gh, Rl, f2_fma(gl, Rh, se));
+  f2_fast_two_sum(sh, se, sh, se);
+}
+
+// A += s d for one component, float-float (s and d float-float, A kept
+// normalised).
+__device__ __forceinline__ void f2_ff_accumulate(float2& Ah, float2& Al, float2 sh, float2 se, float2 dh, float2 dl) {
+  float2 ah, ae;
+  f2_two_prod(sh, dh, ah, ae);
+  ae = f2_fma(sh, dl, f2_fma(se, dh, ae));
+  float2 s1, s2;
+  f2_two_sum(Ah, ah, s1, s2);
+  s2 = f2_add(s2, f2_add(Al, ae));
+  f2_fast_two_sum(s1, s2, Ah, Al);
+}

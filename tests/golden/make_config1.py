@@ -95,10 +95,11 @@ def counters(stderr):
     return dict(accepted=calls, rejected=rejected, evaluations=evals)
 
 
-def run(ref_root="/root/reference"):
+def run(ref_root=None):
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.dirname(HERE))
     import oracle
+    ref_root = ref_root or oracle.REFERENCE_SRC
     from scenario_files import read_affairs, read_integrals
     xml = os.path.join(SCENARIOS, NAME + ".xml")
     write_xml(xml)

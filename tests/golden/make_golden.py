@@ -109,7 +109,7 @@ def small_self_gravitating(seed, n):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=oracle.REFERENCE_SRC)
     ap.add_argument("--skip-full", action="store_true", help="skip the full-size (65,536 body) checksum fixture")
     args = ap.parse_args()
     if not oracle.build_reference(args.ref):

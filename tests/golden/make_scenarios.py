@@ -6,7 +6,7 @@ For every <name>.xml the program runs in a scratch directory (it writes its
 outputs next to the input file) and every output file but the time-stamped
 log is copied to tests/golden/scenarios/<name>/.
 
-    python tests/golden/make_scenarios.py [/root/reference]
+    python tests/golden/make_scenarios.py [reference source root; default $SOLARIS_REFERENCE_SRC]
 """
 import os
 import shutil
@@ -19,9 +19,10 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 SCENARIOS = os.path.join(HERE, "scenarios")
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
     sys.path.insert(0, ROOT)
     import oracle
+    ref_root = ref_root or oracle.REFERENCE_SRC
     if not oracle.build_reference(ref_root):
         raise SystemExit("the reference sources are not available")
     prog = os.path.join(oracle.REF_DIR, "solaris")

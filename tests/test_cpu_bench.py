@@ -47,3 +47,24 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1  # rank 0 alone prints
     _check(lines[0])
     assert lines[0]["n_gpus"] == 2
+
+
+def test_gpus_flag_without_torchrun_starts_the_ranks_itself():
+    """`bench.py --gpus 2` as a plain process runs again as two ranks of
+    torch.distributed.run (rank 0 prints the one line with n_gpus 2)."""
+    pytest.importorskip("torch.distributed.run")
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, "bench.py", "--gpus", "2", *ARGS], cwd=ROOT, capture_output=True, text=True,
+                       timeout=900, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _lines(r.stdout)
+    assert len(lines) == 1 and lines[0]["n_gpus"] == 2
+    _check(lines[0])
+
+
+def test_gpus_flag_must_match_the_world_size():
+    env = dict(os.environ, WORLD_SIZE="3", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, "bench.py", "--gpus", "2", *ARGS], cwd=ROOT, capture_output=True, text=True,
+                       timeout=300, env=env)
+    assert r.returncode != 0
+    assert "WORLD_SIZE=3" in r.stderr

@@ -7,10 +7,11 @@ import subprocess
 
 import pytest
 
+import oracle
 from facade_io import compile_program
 from solaris_gb300 import build
 
-REF = "/root/reference"
+REF = oracle.REFERENCE_SRC
 
 
 def _defined_symbols(path):
