@@ -155,6 +155,51 @@ def profile_figures(name="pair_kernels_65536.md"):
     return out
 
 
+FF_FP32_OPS_PER_PAIR = 116
+# The FP32 pipe completes 128 lane operations per SM cycle (4 sub-partitions x
+# 32 lanes; a paired FFMA2 instruction is two).
+FP32_LANES_PER_SM_CYCLE = 128.0
+
+
+def fp32_peak(local, clocks):
+    """FP32 lane-operation peak (per second) at the SM clock sampled during the
+    timed region, and the probe's measured chains beside it."""
+    import torch
+    from solaris_gb300 import engine
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    probe = engine.fp32_pipe_rates(local)
+    mhz = (clocks or {}).get("sm_mhz") or probe["sm_mhz"] or 2070.0
+    peak = FP32_LANES_PER_SM_CYCLE * nsm * mhz * 1e6
+    return peak, {"sms": nsm, "sm_mhz": mhz, "lanes_per_sm_cycle": FP32_LANES_PER_SM_CYCLE,
+                  "probe_ffma_per_s": probe["ffma"], "probe_ffma2_per_s": probe["ffma2"],
+                  "probe_sm_mhz": probe["sm_mhz"],
+                  "probe_frac_of_peak": max(probe["ffma"], probe["ffma2"]) /
+                  (FP32_LANES_PER_SM_CYCLE * nsm * (probe["sm_mhz"] or mhz) * 1e6)}
+
+
+def roofline_entry(name, pps, fp64_ops, fp32_ops, peak64, info64, peak32, info32, prof, ms):
+    """The dominant kernel's roofline: SPLIT_FF's pair kernel is bound by the
+    FP32 pipe, the other forms by the FP64 pipe."""
+    traffic = {"traffic": prof.get(f"{name}_dram_bytes_per_launch"),
+               "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the pair kernel and its "
+                               "k_combine at 65,536 bodies (profiles/pair_kernels_65536.md)",
+               "kernel_ms_per_launch": ms}
+    if name in fp32_ops:
+        return {"bound": "fp32", "kernel": "k_pairs_ff (SPLIT_FF pair kernel) + k_combine",
+                "achieved": pps * fp32_ops[name] / 1e9, "peak": peak32 / 1e9, "unit": "Gop/s",
+                "frac": pps * fp32_ops[name] / peak32, **traffic, "fp32_ops_per_pair": fp32_ops[name],
+                "fp64_instructions_per_pair_ncu": prof.get(f"{name}_fp64_instructions_per_pair"),
+                "peak_source": "FP32 pipe, 128 lane operations per SM cycle x SMs x the SM clock sampled during "
+                               "the timed region (probe of FFMA / FFMA2 chains beside it)",
+                "peak_detail": info32}
+    return {"bound": "fp64", "kernel": f"k_pairs<{name.upper()}> (pair kernel)",
+            "achieved": pps * fp64_ops[name] / 1e9, "peak": peak64 / 1e9, "unit": "Gop/s",
+            "frac": pps * fp64_ops[name] / peak64, **traffic, "fp64_instructions_per_pair": fp64_ops[name],
+            "peak_source": "FP64 pipe issue rate, 2 thread instructions per SM cycle (ncu peak_sustained 1/16 warp "
+                           "instruction), x SMs x the SM clock sampled during the timed region",
+            "peak_detail": info64}
+
+
 # The FP64 pipe issues 1/16 warp instruction per SM cycle (ncu
 # sm__inst_executed_pipe_fp64.avg.peak_sustained = 0.0625 on the GB300):
 # 2 thread instructions per SM per cycle.
@@ -572,12 +617,17 @@ def main():
                  (("split_ff", abi.PRECISION_SPLIT_FF, 5), ("split", abi.PRECISION_SPLIT, 2),
                   ("fp64", abi.PRECISION_FP64, 2))}
     peak_ops, peak_info = fp64_peak(local, ff["clocks"])  # FP64 thread instructions per second
+    peak32, peak32_info = fp32_peak(local, ff["clocks"])  # FP32 lane operations per second
     # FP64 instructions per pair of each form's arithmetic: SPLIT_FF the 3
     # displacement subtractions; SPLIT 16 (displacement, r^2, the Newton
     # correction with G m, the accumulation); the reference form 14 in the pair
     # (correctly rounded sqrt and reciprocal by one FMA remainder each, the six
     # term multiplies on the integer pipe) plus the 3 in-order additions
-    fp64_ops = {"split_ff": 3, "split": 16, "fp64": 17}
+    fp64_ops = {"split_ff": 0, "split": 16, "fp64": 17}
+    # SPLIT_FF's pair (k_pairs_ff) runs on the FP32 pipe: FP32 lane operations
+    # per pair of its float-float arithmetic (sol_pair.cuh): the displacement
+    # from the grid triples 21, r^2 25, G m r^-3 25, the accumulation 45
+    fp32_ops = {"split_ff": FF_FP32_OPS_PER_PAIR}
     prof = profile_figures()
 
     # end to end through the C-ABI: pinned host state in, host state out, every step
@@ -608,6 +658,8 @@ def main():
                        "fp64_instructions_per_pair": fp64_ops[name],
                        "fp64_instructions_per_pair_ncu": prof.get(f"{name}_fp64_instructions_per_pair"),
                        "fp64_pipe_frac": pps * fp64_ops[name] / peak_ops,
+                       "fp32_ops_per_pair": fp32_ops.get(name),
+                       "fp32_pipe_frac": pps * fp32_ops[name] / peak32 if name in fp32_ops else None,
                        "conventional_tflops": pps * FLOP_PER_PAIR / 1e12,
                        "conventional_frac_of_fp64_peak": pps * FLOP_PER_PAIR / (2.0 * peak_ops),
                        "energy_drift": r["energy_drift"], "steps": r.get("k")}
@@ -641,17 +693,8 @@ def main():
         "accuracy": {"bound": 1e-12, "reference_form": "fp64 (bit-identical to the reference CPU build)",
                      "split_ff_max_rel_accel_err": acc["split_ff"][0], "split_max_rel_accel_err": acc["split"][0],
                      "headline_within_bound": acc[head_name][0] <= 1e-12},
-        "roofline": {"bound": "fp64", "kernel": f"k_pairs<{head_name.upper()}> (pair kernel)",
-                     "achieved": pps_head * fp64_ops[head_name] / 1e9, "peak": peak_ops / 1e9, "unit": "Gop/s",
-                     "frac": pps_head * fp64_ops[head_name] / peak_ops,
-                     "traffic": prof.get(f"{head_name}_dram_bytes_per_launch"),
-                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the pair kernel and "
-                                     "k_combine at 65,536 bodies (profiles/pair_kernels_65536.md)",
-                     "fp64_instructions_per_pair": fp64_ops[head_name],
-                     "kernel_ms_per_launch": ms_launch[head_name],
-                     "peak_source": "FP64 pipe issue rate, 2 thread instructions per SM cycle (ncu peak_sustained "
-                                    "1/16 warp instruction), x SMs x the SM clock sampled during the timed region",
-                     "peak_detail": peak_info},
+        "roofline": roofline_entry(head_name, pps_head, fp64_ops, fp32_ops, peak_ops, peak_info, peak32,
+                                   peak32_info, prof, ms_launch[head_name]),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * 6 * s.n, "d2h_bytes_per_step": 8 * 6 * s.n,
                 "steps": ke, "api": "sol_driver_host (pinned host y0 in/out)"},

@@ -522,6 +522,11 @@ int sol_measure_fp64_peak(int32_t device, double* flops);
  * CTA).  On the GB300 such chains reach 84% of the FP64 pipe's issue rate
  * (1/16 warp instruction per SM cycle). */
 int sol_measure_fp64_pipe(int32_t device, double rates[3], double* sm_mhz);
+/* Measured FP32 pipe throughput in FP32 lane operations per second (an FMA
+ * is one): rates[0] scalar FFMA chains, rates[1] paired FFMA2 chains (two
+ * lanes per instruction), set up as sol_measure_fp64_pipe's; sm_mhz (may be
+ * NULL) the SM clock of the fastest FFMA2 launch. */
+int sol_measure_fp32_pipe(int32_t device, double rates[2], double* sm_mhz);
 /* Self-check of the reference-form pair arithmetic: the correctly rounded
  * sqrt(a) and 1 / (a sqrt(a)) that replace IEEE square root and division in
  * every FP64 GravityAC pair (Acceleration.cpp:294-317), and the integer-pipe

@@ -194,6 +194,7 @@ def _declare(lib):
         "sol_integrals": (C.c_int, [P, _PF64, _PF64]),
         "sol_measure_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
         "sol_measure_fp64_pipe": (C.c_int, [C.c_int32, _PF64, C.POINTER(C.c_double)]),
+        "sol_measure_fp32_pipe": (C.c_int, [C.c_int32, _PF64, C.POINTER(C.c_double)]),
         "sol_check_pair_math": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]),
         "sol_kernel_launch_count": (C.c_int, [C.POINTER(C.c_int64)]),
         "sol_get_stream": (C.c_int, [P, C.POINTER(C.c_void_p)]),
@@ -257,7 +258,7 @@ def exported_names():
         "sol_set_precision", "sol_set_eval_flags", "sol_get_n_total", "sol_accel_compute", "sol_get_mig_type",
         "sol_set_state", "sol_get_state", "sol_set_tolerance", "sol_set_device_loop", "sol_driver", "sol_driver_host",
         "sol_rkf78_step", "sol_get_last_eval", "sol_check_events", "sol_integrals", "sol_measure_fp64_peak",
-        "sol_measure_fp64_pipe", "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc",
+        "sol_measure_fp64_pipe", "sol_measure_fp32_pipe", "sol_kernel_launch_count", "sol_get_stream", "sol_bench_force", "sol_gravity_noalloc",
         "sol_gravity_noalloc_status", "sol_set_wait_test", "sol_accel_sinks_device",
         "sol_ensemble_create", "sol_ensemble_destroy", "sol_ensemble_set_precision", "sol_ensemble_set_tolerance",
         "sol_ensemble_set_state", "sol_ensemble_get_state", "sol_ensemble_advance", "sol_ensemble_configure",

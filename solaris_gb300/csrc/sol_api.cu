@@ -959,6 +959,11 @@ int sol_set_wait_test(sol_ctx* c, uint32_t spin_limit, int32_t withhold) {
   return SOL_OK;
 }
 
+int sol_measure_fp32_pipe(int32_t device, double rates[2], double* sm_mhz) {
+  if (!rates) return SOL_ERR_ARG;
+  return sol_fp32_rates_launch(device, rates, sm_mhz);
+}
+
 int sol_measure_fp64_pipe(int32_t device, double rates[3], double* sm_mhz) {
   if (!rates) return SOL_ERR_ARG;
   return sol_fp64_rates_launch(device, rates, sm_mhz);

@@ -118,6 +118,38 @@ __global__ void __launch_bounds__(kRateThreads) k_fp64_rate(double b, double c, 
   }
 }
 
+// FP32 pipe throughput: OP 0 scalar FFMA chains, OP 1 paired FFMA2 chains
+// (two lanes per instruction), kRateChains per thread as above; the rate is
+// counted in FP32 lane operations (an FFMA2 is two).
+template <int OP>
+__global__ void __launch_bounds__(kRateThreads) k_fp32_rate(float b, float c, float* out, long long* cycles,
+                                                            int iters) {
+  float2 v[kRateChains];
+#pragma unroll
+  for (int k = 0; k < kRateChains; ++k) v[k] = make_float2(1.0f + threadIdx.x * 1e-7f + k * 1e-4f, 1.0f - k * 1e-4f);
+  const long long t0 = clock64();
+  unsigned long long g0 = 0, g1 = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g0));
+  const float2 b2 = make_float2(b, b), c2 = make_float2(c, c);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int k = 0; k < kRateChains; ++k) {
+      if constexpr (OP == 0) v[k].x = __fmaf_rn(v[k].x, b, c);
+      if constexpr (OP == 1) v[k] = __ffma2_rn(v[k], b2, c2);
+    }
+  }
+  const long long t1 = clock64();
+  if (blockIdx.x == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
+  float s = 0;
+#pragma unroll
+  for (int k = 0; k < kRateChains; ++k) s += v[k].x + v[k].y;
+  if (s == -12345.0f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cycles[0] = t1 - t0;
+    cycles[1] = (long long)(g1 - g0);
+  }
+}
+
 // Self-check of sol_ref_rinv3 (correctly rounded sqrt and 1 / (a sqrt a))
 // and of its reciprocal step against IEEE sqrt and division, on seeded
 // samples (splitmix64 of the sample index):
@@ -335,6 +367,60 @@ int sol_fp64_rates_launch(int device, double rates[3], double* sm_mhz) {
   cudaFree(out);
   cudaFree(cyc);
   if (rc == SOL_OK && sm_mhz) *sm_mhz = mhz[0];
+  return rc;
+}
+
+namespace {
+template <int OP>
+int fp32_rate_one(int nsm, float* out, long long* d_cycles, double* rate, double* mhz) {
+  int per_sm = 0;
+  SOL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fp32_rate<OP>, kRateThreads, 0));
+  if (per_sm < 1) per_sm = 1;
+  const int blocks = nsm * per_sm, iters = 65536;
+  const float b = 1.0f - 1.0f / 4096.0f, c = 1.0f / 4096.0f;
+  cudaEvent_t e0, e1;
+  SOL_CUDA(cudaEventCreate(&e0));
+  SOL_CUDA(cudaEventCreate(&e1));
+  k_fp32_rate<OP><<<blocks, kRateThreads>>>(b, c, out, d_cycles, 4096);  // warm-up
+  SOL_LAUNCHED();
+  float best = 1e30f;
+  long long best_cycles[2] = {0, 1};
+  for (int rep = 0; rep < 5; ++rep) {
+    SOL_CUDA(cudaEventRecord(e0));
+    k_fp32_rate<OP><<<blocks, kRateThreads>>>(b, c, out, d_cycles, iters);
+    SOL_LAUNCHED();
+    SOL_CUDA(cudaEventRecord(e1));
+    SOL_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    SOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) {
+      best = ms;
+      SOL_CUDA(cudaMemcpy(best_cycles, d_cycles, 2 * sizeof(long long), cudaMemcpyDeviceToHost));
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double lanes = OP == 1 ? 2.0 : 1.0;
+  *rate = lanes * (double)blocks * kRateThreads * kRateChains * iters / (best * 1e-3);
+  *mhz = best_cycles[1] > 0 ? 1e3 * (double)best_cycles[0] / (double)best_cycles[1] : 0.0;
+  return SOL_OK;
+}
+}  // namespace
+
+int sol_fp32_rates_launch(int device, double rates[2], double* sm_mhz) {
+  SOL_CUDA(cudaSetDevice(device));
+  int nsm = 0;
+  SOL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+  float* out = nullptr;
+  long long* cyc = nullptr;
+  SOL_CUDA(cudaMalloc(&out, sizeof(float) * (size_t)nsm * 32 * kRateThreads));
+  SOL_CUDA(cudaMalloc(&cyc, 2 * sizeof(long long)));
+  double mhz[2] = {0, 0};
+  int rc = fp32_rate_one<0>(nsm, out, cyc, &rates[0], &mhz[0]);
+  if (rc == SOL_OK) rc = fp32_rate_one<1>(nsm, out, cyc, &rates[1], &mhz[1]);
+  cudaFree(out);
+  cudaFree(cyc);
+  if (rc == SOL_OK && sm_mhz) *sm_mhz = mhz[1];
   return rc;
 }
 

@@ -217,6 +217,7 @@ int sol_group_rkf78(sol_ctx* c, int n_steps, const GroupSim* sim = nullptr, int 
 int sol_fp64_peak_launch(int device, double* flops);
 void sol_noalloc_wait_test(unsigned spin_limit, int withhold_tile);
 int sol_fp64_rates_launch(int device, double rates[3], double* sm_mhz);
+int sol_fp32_rates_launch(int device, double rates[2], double* sm_mhz);
 int sol_check_pair_math_launch(int device, int mode, long long n, unsigned long long seed, long long* result);
 
 // ---- PTX helpers: bulk copies (TMA engine) with mbarrier completion --------

@@ -148,16 +148,28 @@ __device__ __forceinline__ void f2_two_prod(float2 a, float2 b, float2& p, float
 //   d = (a_j - a_i) + (b_j - b_i) + (c_j - c_i)
 // is formed as a float-float (h, l) with an absolute error below ~2^-22 G2,
 // i.e. 2^-46 |d| for |d| >= G1 / 2: the FastTwoSum of the two exact parts
-// (|a_j - a_i| >= G1 >= |b_j - b_i| unless a_j = a_i), the rounded c part
-// added to the low word, one more FastTwoSum.  No FP64 instruction.
+// (|a_j - a_i| >= G1 >= |b_j - b_i| unless a_j = a_i) and the rounded c part
+// added to its low word.  For |d| >= G1 (every pair this form serves) the
+// low word stays below 2^-23 |h| (half an ulp of h plus |c_j - c_i| <= G2),
+// close enough to normalised for the products that follow.  No FP64
+// instruction.
 __device__ __forceinline__ void f2_grid_disp(float2 aj, float2 bj, float2 cj, float ai, float bi, float ci, float2& h,
                                              float2& l) {
   const float2 s1 = f2_sub(aj, f2_splat(ai));
   const float2 s2 = f2_sub(bj, f2_splat(bi));
   const float2 s3 = f2_sub(cj, f2_splat(ci));
-  float2 hh, l0;
-  f2_fast_two_sum(s1, s2, hh, l0);
-  f2_fast_two_sum(hh, f2_add(l0, s3), h, l);
+  float2 l0;
+  f2_fast_two_sum(s1, s2, h, l0);
+  l = f2_add(l0, s3);
+}
+
+// TwoSum of two non-negative numbers: FastTwoSum with the larger first (the
+// ordering by max / min runs on the integer pipe).
+__device__ __forceinline__ void f2_two_sum_pos(float2 a, float2 b, float2& s, float2& e) {
+  const float2 big = make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y));
+  const float2 small = make_float2(fminf(a.x, b.x), fminf(a.y, b.y));
+  s = f2_add(a, b);
+  e = f2_add(f2_sub(big, s), small);
 }
 
 // r^2 = sum_k (h_k + l_k)^2 as a float-float (exact squares of the high
@@ -168,8 +180,8 @@ __device__ __forceinline__ void f2_ff_r2(const float2* h, const float2* l, float
 #pragma unroll
   for (int k = 0; k < 3; ++k) f2_two_prod(h[k], h[k], p[k], e[k]);
   float2 s12, t12, s3, t3;
-  f2_two_sum(p[0], p[1], s12, t12);
-  f2_two_sum(s12, p[2], s3, t3);
+  f2_two_sum_pos(p[0], p[1], s12, t12);
+  f2_two_sum_pos(s12, p[2], s3, t3);
   float2 lo = f2_add(f2_add(t12, t3), f2_add(f2_add(e[0], e[1]), e[2]));
 #pragma unroll
   for (int k = 0; k < 3; ++k) lo = f2_fma(f2_add(h[k], h[k]), l[k], lo);

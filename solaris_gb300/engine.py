@@ -301,6 +301,17 @@ def fp64_pipe_rates(device: int = 0) -> dict:
     return {"dfma": float(r[0]), "dadd": float(r[1]), "dmul": float(r[2]), "sm_mhz": float(mhz.value)}
 
 
+def fp32_pipe_rates(device: int = 0) -> dict:
+    """FP32 pipe throughput of this GPU (sol_measure_fp32_pipe): FP32 lane
+    operations per second of scalar FFMA and paired FFMA2 chains, and the SM
+    clock (MHz) of the FFMA2 measurement."""
+    lib = abi.load_library()
+    r = (C.c_double * 2)()
+    mhz = C.c_double(0)
+    abi.check(lib, lib.sol_measure_fp32_pipe(int(device), r, C.byref(mhz)))
+    return {"ffma": float(r[0]), "ffma2": float(r[1]), "sm_mhz": float(mhz.value)}
+
+
 def check_pair_math(mode: int, n: int, seed: int = 1, device: int = 0) -> dict:
     """Self-check of the correctly rounded sqrt / reciprocal of the FP64 pair
     against IEEE sqrt and division (sol_check_pair_math): mismatches (0 when

@@ -12,6 +12,8 @@ Cases (each holds a few hundred MB of device memory at most):
   split_ff_2d     k_pairs<SPLIT_FF> + k_combine: float-float force, 32,768 bodies
   fp64_rate       k_fp64_rate<0,1,2>: the FP64 pipe throughput probe (DFMA,
                   DADD, DMUL chains), prints the rates and the SM clock
+  fp32_rate       k_fp32_rate<0,1>: the FP32 pipe throughput probe (FFMA,
+                  FFMA2 chains)
   persistent      k_group_rkf78: 20 RKF78 driver calls of 1 star + 2 giants +
                   253 test particles in one cooperative launch
   ensemble        k_ensemble_rkf78: 2 driver calls of 512 small systems
@@ -50,6 +52,8 @@ def run(case: str) -> None:
             ctx.accel(0.0, s.y0)
     elif case == "fp64_rate":
         print(engine.fp64_pipe_rates(0))
+    elif case == "fp32_rate":
+        print(engine.fp32_pipe_rates(0))
     elif case == "persistent":
         s = scenarios.config1()
         with engine.Context(s) as ctx:
