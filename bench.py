@@ -137,13 +137,20 @@ def run_reference(args, rank, world):
     replicas.finalize()
 
 
-def profile_figures(name="pair_kernels_65536.md"):
-    """`key: value` lines of a committed ncu summary (DRAM bytes per launch,
-    FP64 instructions per pair measured at the bench size)."""
-    p = os.path.join(ROOT, "profiles", name)
+def profile_figures(names=("pair_kernels_65536.md", "k_pairs_ff_65536.md")):
+    """`key: value` lines of the committed ncu summaries (DRAM bytes per
+    launch, instructions per pair measured at the bench size); later files
+    override earlier ones."""
     out = {}
-    if not os.path.exists(p):
-        return out
+    for name in names:
+        p = os.path.join(ROOT, "profiles", name)
+        if os.path.exists(p):
+            out.update(_figures(p))
+    return out
+
+
+def _figures(p):
+    out = {}
     for line in open(p):
         line = line.strip().lstrip("-* ")
         if ":" in line and line.split(":", 1)[0].replace("_", "").isalnum():
@@ -182,7 +189,8 @@ def roofline_entry(name, pps, fp64_ops, fp32_ops, peak64, info64, peak32, info32
     FP32 pipe, the other forms by the FP64 pipe."""
     traffic = {"traffic": prof.get(f"{name}_dram_bytes_per_launch"),
                "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the pair kernel and its "
-                               "k_combine at 65,536 bodies (profiles/pair_kernels_65536.md)",
+                               "k_combine at 65,536 bodies (profiles/pair_kernels_65536.md, "
+                               "profiles/k_pairs_ff_65536.md)",
                "kernel_ms_per_launch": ms}
     if name in fp32_ops:
         return {"bound": "fp32", "kernel": "k_pairs_ff (SPLIT_FF pair kernel) + k_combine",
