@@ -63,6 +63,7 @@ def load():
         lib.orc_n_total.argtypes = [P]
         lib.orc_set_eval_flags.argtypes = [P, C.c_uint32]
         lib.orc_set_epsilon.argtypes = [P, C.c_double]
+        lib.orc_set_threads.argtypes = [P, C.c_int32]
         lib.orc_compute.argtypes = [P, C.c_double, F, F]
         lib.orc_get_last_eval.argtypes = [P, F, I, F]
         lib.orc_get_mig_type.argtypes = [P, I]
@@ -107,6 +108,11 @@ class Oracle:
         if getattr(self, "h", None):
             self.lib.orc_destroy(self.h)
             self.h = None
+
+    def set_threads(self, n_threads):
+        """Host threads of the force and tangent-linear sink loops (default 1;
+        the results do not depend on it)."""
+        self.lib.orc_set_threads(self.h, int(n_threads))
 
     def set_eval_flags(self, flags):
         self.lib.orc_set_eval_flags(self.h, flags)

@@ -71,6 +71,9 @@ struct orc_system {
   double epsilon;
   /* integrator scratch */
   double *accel, *yscale, *error, *ytmp, *ybuf, *fk[13];
+  /* host threads of the sink loops of GravityAC and of orc_jvp (default 1;
+   * every sink's sum stays sequential, so the results do not depend on it) */
+  int n_threads;
 };
 
 static int n_massive(const orc_system* s) {
@@ -91,6 +94,7 @@ static int32_t* dup_i(const int32_t* src, int n, int32_t fill) {
 
 orc_system* orc_create(const sol_body_data* b, const sol_gas_component* gas, int32_t barycentric) {
   orc_system* s = (orc_system*)calloc(1, sizeof(orc_system));
+  s->n_threads = 1;
   s->n = b->n;
   s->total = b->n.central_body + b->n.giant_planet + b->n.rocky_planet + b->n.proto_planet +
              b->n.super_planetesimal + b->n.planetesimal + b->n.test_particle;
@@ -354,8 +358,13 @@ static void gravity_ac(orc_system* s, const double* y, double* accel) {
   gravity_ac_prepass(s, y);
   accel[0] = accel[1] = accel[2] = accel[3] = accel[4] = accel[5] = 0.0;
   int nm = n_massive(s);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(s->n_threads) if (s->n_threads > 1)
+#endif
   for (int i = 1; i < s->total; i++) gravity_ac_sink(s, y, accel, i, nm);
 }
+
+void orc_set_threads(orc_system* s, int32_t n_threads) { s->n_threads = n_threads > 1 ? n_threads : 1; }
 
 static void gravity_bc_range(orc_system* s, const double* y, double* accel, int lo, int hi) {
   /* GravityBC_SelfInteracting / _NonSelfInteracting, Acceleration.cpp:541-634 */
@@ -999,6 +1008,9 @@ void orc_jvp(orc_system* s, const double* y, const double* dy, const double* dm,
   int N = s->total, nm = n_massive(s), nspl = s->n.super_planetesimal;
   double m0 = s->mass[0], dm0 = dm ? dm[0] : 0.0;
   for (int k = 0; k < 6; ++k) df[k] = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(s->n_threads) if (s->n_threads > 1)
+#endif
   for (int i = 1; i < N; ++i) {
     const double* ri = &y[6 * i];
     const double* dri = &dy[6 * i];

@@ -26,6 +26,8 @@ void orc_destroy(orc_system* s);
 int32_t orc_n_total(const orc_system* s);
 void orc_set_eval_flags(orc_system* s, uint32_t flags);
 void orc_set_epsilon(orc_system* s, double eps);
+/* host threads of the sink loops of GravityAC and orc_jvp (default 1) */
+void orc_set_threads(orc_system* s, int32_t n_threads);
 
 /* Acceleration::Compute (Solaris/Acceleration.cpp:60-80). */
 int orc_compute(orc_system* s, double t, const double* y, double* dydt);

@@ -11,8 +11,8 @@
 #include "sol_internal.cuh"
 
 int sol_force_tile();
-int sol_force_part_doubles(int npad);
-int sol_force_uses_chunk_partials(const sol_ctx* c);
+int sol_force_part_doubles(const sol_ctx* c);
+int sol_force_uses_chunk_partials(const sol_ctx* c, int precision);
 int sol_force_prepass_blocks(int npad);
 int sol_force_src_doubles();
 int sol_force_launch_sinks(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int lo, int hi);
@@ -395,9 +395,9 @@ int sol_set_precision(sol_ctx* c, int32_t p) {
     sol_set_error("precision %d: barycentric contexts compute in FP64 only", p);
     return SOL_ERR_ARG;
   }
-  if (p != SOL_PRECISION_FP64 && !c->barycentric && !c->d_part && sol_force_uses_chunk_partials(c)) {
+  if (p != SOL_PRECISION_FP64 && !c->barycentric && !c->d_part && sol_force_uses_chunk_partials(c, p)) {
     RET(set_device(c));
-    RET(dev_alloc(&c->d_part, (size_t)sol_force_part_doubles(c->npad)));
+    RET(dev_alloc(&c->d_part, (size_t)sol_force_part_doubles(c)));
   }
   c->precision = p;
   c->fc.precision = p;

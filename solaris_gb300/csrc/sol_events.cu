@@ -254,8 +254,8 @@ __global__ void k_gather_rows(int lo_old, int hi_old, int lo_new, const int* __r
 
 }  // namespace
 
-int sol_force_part_doubles(int npad);
-int sol_force_uses_chunk_partials(const sol_ctx* c);
+int sol_force_part_doubles(const sol_ctx* c);
+int sol_force_uses_chunk_partials(const sol_ctx* c, int precision);
 
 extern "C" int sol_handle_events(sol_ctx* c, double time, double ejection, double hit_centrum,
                                  double collision_factor, sol_affair* log, int32_t capacity, int32_t* n_log) {
@@ -423,8 +423,8 @@ extern "C" int sol_handle_events(sol_ctx* c, double time, double ejection, doubl
       c->fc.has_mig2 = nw.n_giant > 0 && c->fc.has_mig2;
       for (int g = 0; g < 2; ++g) sol_graph_release(c->graphs[g]);  // captured with the old body count
       // a smaller system may move to the 2-D split kernel, which needs its partials
-      if (c->precision != SOL_PRECISION_FP64 && !c->d_part && sol_force_uses_chunk_partials(c)) {
-        if (cudaMalloc((void**)&c->d_part, sizeof(double) * (size_t)sol_force_part_doubles(c->npad)) != cudaSuccess) {
+      if (c->precision != SOL_PRECISION_FP64 && !c->d_part && sol_force_uses_chunk_partials(c, c->precision)) {
+        if (cudaMalloc((void**)&c->d_part, sizeof(double) * (size_t)sol_force_part_doubles(c)) != cudaSuccess) {
           sol_set_error("cudaMalloc of the split partials failed");
           rc = SOL_ERR_NOMEM;
         }

@@ -21,7 +21,7 @@
 #include "sol_crmath.cuh"
 #include "sol_pair.cuh"
 
-int sol_force_uses_chunk_partials(const sol_ctx* c);
+int sol_force_uses_chunk_partials(const sol_ctx* c, int precision);
 
 namespace {
 
@@ -832,7 +832,7 @@ __device__ __forceinline__ void pair_ff(const double* __restrict__ sx, const dou
 // block scheduler balance the FP64 pipe load across SMs.
 template <int MODE>
 __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double* __restrict__ y,
-                                                      double* __restrict__ part, int* dev_status) {
+                                                      double* __restrict__ part, int* dev_status, int chunk) {
   constexpr int NARR = 4;  // x, y, z and G m (FP64 for SPLIT, float-float for SPLIT_FF)
   __shared__ __align__(128) TileSmem<NARR> sm;
   const Classes& c = fc.cls;
@@ -842,8 +842,8 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
   const int i_first = fc.sink_lo + blockIdx.x * kSinkBlock;
   const int ns_cta = (fc.type[min(i_first, n - 1)] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
   const int ns = (i < n && fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
-  const int j_begin = blockIdx.y * kChunk;
-  const int j_end = min(j_begin + kChunk, ns_cta);
+  const int j_begin = blockIdx.y * chunk;
+  const int j_end = min(j_begin + chunk, ns_cta);
   const int t_begin = j_begin / kTile;
   const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
   const int arr[NARR] = {SX, SY, SZ, MODE == SOL_PRECISION_SPLIT ? SGM : SGF};
@@ -940,7 +940,8 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
 
 // ---- SPLIT_FF 2-D kernel: float-float pairs with no FP64 instruction -------
 // Same grid as k_pairs (blockIdx.x: kSinkBlock sinks; blockIdx.y: a chunk of
-// kChunk sources) and the same partial outputs for k_combine.  The sources'
+// sources, 1 to kChunkTiles tiles as split_chunk chooses so that the grid
+// fills the GPU) and the same partial outputs for k_combine.  The sources'
 // grid triples and G m (hi, lo) arrive tile by tile in shared memory by bulk
 // copies; each thread takes two sources per step in paired FP32
 // instructions: the displacement from the grid triples (exact parts, no
@@ -1030,7 +1031,7 @@ __device__ __forceinline__ void ff_two_sources(const FFTile& sm, int st, int jj,
 }
 
 __global__ void __launch_bounds__(kSinkBlock) k_pairs_ff(ForceCtx fc, const double* __restrict__ y,
-                                                         double* __restrict__ part, int* dev_status) {
+                                                         double* __restrict__ part, int* dev_status, int chunk) {
   __shared__ __align__(128) FFTile sm;
   const Classes& c = fc.cls;
   const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
@@ -1039,8 +1040,8 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs_ff(ForceCtx fc, const doub
   const int i_first = fc.sink_lo + blockIdx.x * kSinkBlock;
   const int ns_cta = (fc.type[min(i_first, n - 1)] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
   const int ns = (i < n && fc.type[i] <= SOL_PROTO_PLANET) ? c.nm + c.n_spl : c.nm;
-  const int j_begin = blockIdx.y * kChunk;
-  const int j_end = min(j_begin + kChunk, ns_cta);
+  const int j_begin = blockIdx.y * chunk;
+  const int j_end = min(j_begin + chunk, ns_cta);
   const int t_begin = j_begin / kTile;
   const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
   const bool live = i < n && i >= 1;
@@ -1228,7 +1229,8 @@ __global__ void k_combine(ForceCtx fc, const double* __restrict__ y, double* __r
 // FP64 instruction runs on full warps: on the GB300 the FP64 pipe is scarce
 // and is charged per warp instruction.
 constexpr int kFewSplitWarps = 8;
-constexpr int kFewSplitMax = 16384;
+constexpr int kFewSplitMax = 16384;  // SPLIT: the warp-per-sink kernel up to here
+constexpr int kFfMinBodies = 4096;   // SPLIT_FF: k_pairs_ff from here (below, the warp-per-sink kernel)
 constexpr int kFoldRounds = 64;
 
 __device__ __forceinline__ void warp_two_sum(double& s, double& c) {
@@ -1379,6 +1381,38 @@ __global__ void __launch_bounds__(kFewSplitWarps * 32) k_pairs_few(ForceCtx fc, 
 }  // namespace
 
 // parts: 1 = prepass (and indirect totals), 2 = pair kernel, 3 = both.
+// Sources per CTA of the 2-D split kernels: SPLIT takes kChunk; SPLIT_FF a
+// chunk of 1..kChunkTiles tiles: among the grids that give every SM at least
+// the four CTAs k_pairs_ff holds, the one whose busiest SM has the least
+// work (its CTAs times the tiles of a CTA plus half a tile of per-CTA work),
+// ties to the larger chunk; the finest chunk when no grid is that large.
+// Small systems fill the GPU, and sizes just past a whole number of CTAs
+// per SM avoid a nearly empty last round.
+static int split_chunk(const sol_ctx* c, int precision) {
+  if (precision != SOL_PRECISION_SPLIT_FF) return kChunk;
+  static int sms[kMaxDevices];
+  const int dev = (c->device >= 0 && c->device < kMaxDevices) ? c->device : 0;
+  if (sms[dev] == 0) {
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 152;
+    sms[dev] = nsm;
+  }
+  const long nb = (c->n + kSinkBlock - 1) / kSinkBlock;
+  const long nsm = sms[dev];
+  int best_ct = 1;
+  double best = 1e300;
+  for (int ct = kChunkTiles; ct >= 1; ct >>= 1) {
+    const long ctas = nb * ((c->n + ct * kTile - 1) / (ct * kTile));
+    if (ctas < 4 * nsm) continue;
+    const double cost = (double)((ctas + nsm - 1) / nsm) * (ct + 0.5);
+    if (cost < best) {
+      best = cost;
+      best_ct = ct;
+    }
+  }
+  return best_ct * kTile;
+}
+
 // The sinks of fc's range [sink_lo, sol_sink_hi) (every body by default);
 // the prepass always covers every body (the sources).
 static int force_launch(sol_ctx* c, const ForceCtx& fc, const double* d_y, double* d_dydt, TimeSpec ts,
@@ -1386,7 +1420,7 @@ static int force_launch(sol_ctx* c, const ForceCtx& fc, const double* d_y, doubl
   const int nsink = sol_sink_hi(fc) - fc.sink_lo;
   const int split = (c->precision != SOL_PRECISION_FP64 && !c->barycentric) ? 1 : 0;
   // SPLIT_FF systems beyond the warp-per-sink kernel run k_pairs_ff on the float table
-  const int ff2d = split && c->precision == SOL_PRECISION_SPLIT_FF && sol_force_uses_chunk_partials(c);
+  const int ff2d = split && c->precision == SOL_PRECISION_SPLIT_FF && sol_force_uses_chunk_partials(c, c->precision);
   if (parts & 1) {
     const int nb_pre = (fc.npad + kPrepassBlock - 1) / kPrepassBlock;
     k_prepass<<<nb_pre, kPrepassBlock, 0, c->stream>>>(fc, d_y, split, ff2d);
@@ -1444,7 +1478,7 @@ static int force_launch(sol_ctx* c, const ForceCtx& fc, const double* d_y, doubl
     SOL_LAUNCHED();
     return SOL_OK;
   }
-  if (split && c->n <= kFewSplitMax && c->cls.nm + c->cls.n_spl >= kTile) {
+  if (split && !sol_force_uses_chunk_partials(c, c->precision)) {
     const int grid = (nsink + kFewSplitWarps - 1) / kFewSplitWarps;
     if (c->precision == SOL_PRECISION_SPLIT_FF)
       k_pairs_few<SOL_PRECISION_SPLIT_FF><<<grid, kFewSplitWarps * 32, 0, c->stream>>>(fc, d_y, d_dydt, ts, flags);
@@ -1458,12 +1492,14 @@ static int force_launch(sol_ctx* c, const ForceCtx& fc, const double* d_y, doubl
       sol_set_error("split precision selected without sol_set_precision");
       return SOL_ERR_STATE;
     }
-    const int nchunk = (c->n + kChunk - 1) / kChunk;
+    const int chunk = split_chunk(c, c->precision);
+    const int nchunk = (c->n + chunk - 1) / chunk;
     dim3 grid(nb, nchunk);
     if (c->precision == SOL_PRECISION_SPLIT_FF)
-      k_pairs_ff<<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status);
+      k_pairs_ff<<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status, chunk);
     else
-      k_pairs<SOL_PRECISION_SPLIT><<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status);
+      k_pairs<SOL_PRECISION_SPLIT><<<grid, kSinkBlock, 0, c->stream>>>(fc, d_y, c->d_part, &c->d_ctrl->dev_status,
+                                                                      chunk);
     SOL_LAUNCHED();
     k_combine<<<(nsink + 255) / 256, 256, 0, c->stream>>>(fc, d_y, d_dydt, c->d_part, nchunk, ts, flags);
   } else {
@@ -1494,11 +1530,18 @@ int sol_force_launch_sinks(sol_ctx* c, const double* d_y, double* d_dydt, TimeSp
 
 int sol_force_tile() { return kTile; }
 int sol_force_src_doubles() { return kSrcDoubles; }
-int sol_force_part_doubles(int npad) { return ((npad + kChunk - 1) / kChunk) * PART_SLOTS * npad; }
+// chunk partials for either split form's 2-D kernel
+int sol_force_part_doubles(const sol_ctx* c) {
+  const int a = (c->n + kChunk - 1) / kChunk;
+  const int ff = split_chunk(c, SOL_PRECISION_SPLIT_FF);
+  const int b = (c->n + ff - 1) / ff;
+  return (a > b ? a : b) * PART_SLOTS * c->npad;
+}
 // whether the split forms of this system run the 2-D kernel (and need its
 // chunk partials); the same test as the dispatch in sol_force_launch_parts
-int sol_force_uses_chunk_partials(const sol_ctx* c) {
-  return !(c->n <= kFewSplitMax && c->cls.nm + c->cls.n_spl >= kTile);
+int sol_force_uses_chunk_partials(const sol_ctx* c, int precision) {
+  const int few_max = precision == SOL_PRECISION_SPLIT_FF ? kFfMinBodies - 1 : kFewSplitMax;
+  return !(c->n <= few_max && c->cls.nm + c->cls.n_spl >= kTile);
 }
 int sol_force_prepass_blocks(int npad) { return (npad + kPrepassBlock - 1) / kPrepassBlock; }
 

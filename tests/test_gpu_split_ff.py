@@ -97,3 +97,19 @@ def test_split_ff_large_kernel_far_from_the_origin():
         nnff = ctx.last_eval()[1]
     assert _rel(dff, d64).max() <= SPLIT_RTOL
     assert np.array_equal(nnff, nn64)
+
+
+@pytest.mark.parametrize("n", [4096, 9000])
+def test_split_ff_small_systems_use_short_chunks(n):
+    """From 4,096 bodies SPLIT_FF runs k_pairs_ff with source chunks of 1 to 16
+    tiles, chosen so that the grid fills the GPU (one or two tiles at these
+    sizes): still within the bound, same nearest neighbours."""
+    s = scenarios.config3(seed=78, n=n)
+    with engine.Context(s, precision=abi.PRECISION_FP64) as ctx:
+        d64, *_ = ctx.accel(0.0, s.y0)
+        nn64 = ctx.last_eval()[1]
+        ctx.set_precision(abi.PRECISION_SPLIT_FF)
+        dff, *_ = ctx.accel(0.0, s.y0)
+        nnff = ctx.last_eval()[1]
+    assert _rel(dff, d64).max() <= SPLIT_RTOL
+    assert np.array_equal(nnff, nn64)
