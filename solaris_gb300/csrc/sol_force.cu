@@ -810,30 +810,17 @@ __global__ void __launch_bounds__(kSinkBlock) k_gravity_bc(ForceCtx fc, const do
 }
 
 
-// Float-float pair of the 2-D kernel: sources from the shared-memory tile,
-// nearest-neighbour candidate tracked on (r^2 hi, r^2 lo).
-__device__ __forceinline__ void pair_ff(const double* __restrict__ sx, const double* __restrict__ sy,
-                                        const double* __restrict__ sz, const float2* __restrict__ sg, int jj, int j,
-                                        int i, int ns, double xi, double yi, double zi, FFAcc& A, double& fbx,
-                                        double& fby, double& fbz, float& mh, float& ml, int& nn) {
-  const float2 g = (j < ns) ? sg[jj] : make_float2(0.0f, 0.0f);  // G m of j = 0 and padding is 0
-  float r2h, r2l;
-  ff_pair_accumulate(sx[jj] - xi, sy[jj] - yi, sz[jj] - zi, g, A, fbx, fby, fbz, r2h, r2l);
-  const bool better = ((r2h < mh) | ((r2h == mh) & (r2l < ml))) & (j >= 1) & (j < ns) & (j != i);
-  mh = better ? r2h : mh;
-  ml = better ? r2l : ml;
-  nn = better ? j : nn;
-}
-
-// 2-D pair kernel of the split forms: blockIdx.x = block of kSinkBlock sinks,
-// blockIdx.y = chunk of kChunk sources.  Each CTA writes, per sink, its
+// 2-D pair kernel of the SPLIT form: blockIdx.x = block of kSinkBlock sinks,
+// blockIdx.y = chunk of `chunk` sources.  Each CTA writes, per sink, its
 // partial acceleration sum and nearest-neighbour candidate for the chunk;
 // k_combine adds the chunks in a fixed order.  Many small work units let the
-// block scheduler balance the FP64 pipe load across SMs.
+// block scheduler balance the FP64 pipe load across SMs.  (SPLIT_FF has its
+// own 2-D kernel, k_pairs_ff.)
 template <int MODE>
 __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double* __restrict__ y,
                                                       double* __restrict__ part, int* dev_status, int chunk) {
-  constexpr int NARR = 4;  // x, y, z and G m (FP64 for SPLIT, float-float for SPLIT_FF)
+  static_assert(MODE == SOL_PRECISION_SPLIT, "k_pairs serves the SPLIT form");
+  constexpr int NARR = 4;  // x, y, z and G m
   __shared__ __align__(128) TileSmem<NARR> sm;
   const Classes& c = fc.cls;
   const int n = sol_sink_hi(fc);  // sinks [sink_lo, n)
@@ -846,7 +833,7 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
   const int j_end = min(j_begin + chunk, ns_cta);
   const int t_begin = j_begin / kTile;
   const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
-  const int arr[NARR] = {SX, SY, SZ, MODE == SOL_PRECISION_SPLIT ? SGM : SGF};
+  const int arr[NARR] = {SX, SY, SZ, SGM};
 
   double xi = 0, yi = 0, zi = 0;
   if (i < n) {
@@ -873,7 +860,6 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
   double ax = 0.0, ay = 0.0, az = 0.0;  // chunk sums of the per-tile partials
   double cx = 0.0, cy = 0.0, cz = 0.0;  // compensation terms
   long long r2minb = __double_as_longlong(1.0e20);
-  float mh = 1.0e20f, ml = 0.0f;
   int nn = -1;
   int issued = ntiles < 2 ? ntiles : 2;
   int t = 0;
@@ -884,30 +870,13 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
     const int j0 = (t_begin + t) * kTile;
     const int jmax = min(kTile, j_end - j0);  // sources beyond the chunk's range are never read
     if (ok && i < n && i >= 1) {
-      if constexpr (MODE == SOL_PRECISION_SPLIT) {
-        double tx = 0.0, ty = 0.0, tz = 0.0;
+      double tx = 0.0, ty = 0.0, tz = 0.0;
 #pragma unroll 4
-        for (int jj = 0; jj < jmax; ++jj)
-          pair_split(*reinterpret_cast<TileSmem<4>*>(&sm), st, jj, j0 + jj, i, ns, xi, yi, zi, tx, ty, tz, r2minb,
-                     nn);
-        two_sum(ax, cx, tx);
-        two_sum(ay, cy, ty);
-        two_sum(az, cz, tz);
-      } else {
-        FFAcc A;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) A.h[k] = A.l[k] = 0.0f;
-        double fbx = 0.0, fby = 0.0, fbz = 0.0;
-        const float2* sg = reinterpret_cast<const float2*>(&sm.v[st][3][0]);
-#pragma unroll 2
-        for (int jj = 0; jj < jmax; ++jj)
-          pair_ff(&sm.v[st][0][0], &sm.v[st][1][0], &sm.v[st][2][0], sg, jj, j0 + jj, i, ns, xi, yi, zi, A, fbx, fby,
-                  fbz, mh, ml, nn);
-        // fold the tile's float-float partial into the FP64 chunk sums
-        two_sum(ax, cx, ((double)A.h[0] + (double)A.l[0]) + fbx);
-        two_sum(ay, cy, ((double)A.h[1] + (double)A.l[1]) + fby);
-        two_sum(az, cz, ((double)A.h[2] + (double)A.l[2]) + fbz);
-      }
+      for (int jj = 0; jj < jmax; ++jj)
+        pair_split(*reinterpret_cast<TileSmem<4>*>(&sm), st, jj, j0 + jj, i, ns, xi, yi, zi, tx, ty, tz, r2minb, nn);
+      two_sum(ax, cx, tx);
+      two_sum(ay, cy, ty);
+      two_sum(az, cz, tz);
     }
     if (__syncthreads_or(!ok)) {
       timed_out = true;
@@ -932,9 +901,7 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs(ForceCtx fc, const double*
   part[base + PAX * np] = ax + cx;
   part[base + PAY * np] = ay + cy;
   part[base + PAZ * np] = az + cz;
-  const double r2min =
-      (MODE == SOL_PRECISION_SPLIT) ? __longlong_as_double(r2minb) : (double)mh + (double)ml;
-  part[base + PR2 * np] = nn >= 0 ? r2min : 1.0e300;
+  part[base + PR2 * np] = nn >= 0 ? __longlong_as_double(r2minb) : 1.0e300;
   part[base + PIDX * np] = __longlong_as_double((long long)nn);
 }
 

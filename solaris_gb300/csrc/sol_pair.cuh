@@ -215,6 +215,8 @@ __device__ __forceinline__ void f2_ff_accumulate(float2& Ah, float2& Al, float2 
   f2_two_prod(sh, dh, ah, ae);
   ae = f2_fma(sh, dl, f2_fma(se, dh, ae));
   float2 s1, s2;
+  // (Knuth's TwoSum: ordering the pair by magnitude instead put a compare and
+  // two selections on this accumulator's serial chain and measured 4% slower)
   f2_two_sum(Ah, ah, s1, s2);
   s2 = f2_add(s2, f2_add(Al, ae));
   f2_fast_two_sum(s1, s2, Ah, Al);
