@@ -626,12 +626,13 @@ def main():
                   ("fp64", abi.PRECISION_FP64, 2))}
     peak_ops, peak_info = fp64_peak(local, ff["clocks"])  # FP64 thread instructions per second
     peak32, peak32_info = fp32_peak(local, ff["clocks"])  # FP32 lane operations per second
-    # FP64 instructions per pair of each form's arithmetic: SPLIT_FF the 3
-    # displacement subtractions; SPLIT 16 (displacement, r^2, the Newton
-    # correction with G m, the accumulation); the reference form 14 in the pair
-    # (correctly rounded sqrt and reciprocal by one FMA remainder each, the six
-    # term multiplies on the integer pipe) plus the 3 in-order additions
-    fp64_ops = {"split_ff": 0, "split": 16, "fp64": 17}
+    # FP64 instructions per pair of each form's arithmetic: SPLIT_FF none (its
+    # pair runs on the FP32 pipe); SPLIT 13 (displacement 3, r^2 3, the Newton
+    # residual and correction 2, G m y^3 corr 2, the accumulation 3; the seed's
+    # square and cube come from the integer pipe); the reference form 14 in the
+    # pair (correctly rounded sqrt and reciprocal by one FMA remainder each,
+    # the six term multiplies on the integer pipe) plus the 3 in-order additions
+    fp64_ops = {"split_ff": 0, "split": 13, "fp64": 17}
     # SPLIT_FF's pair (k_pairs_ff) runs on the FP32 pipe: FP32 lane operations
     # per pair of its float-float arithmetic (sol_pair.cuh): the displacement
     # from the grid triples 21, r^2 25, G m r^-3 25, the accumulation 45

@@ -217,12 +217,61 @@ __device__ __forceinline__ void pair_fp64(const TileSmem<7>& sm, int st, int jj,
   }
 }
 
+// The FP32 seed y (positive, normal) as y^2 and y^3 in FP64 without FP64
+// instructions: from y's 24-bit significand m by integer multiplies, y^2 =
+// m^2 (48 bits, exact) and y^3 = m^3 (72 bits, truncated to 53), with the
+// exponents set directly.
+__device__ __forceinline__ void seed_square_cube(float yf, double& u, double& y3) {
+  const unsigned b = __float_as_uint(yf);
+  const int E = (int)(b >> 23) - 127;  // yf = 2^E m 2^-23
+  const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
+  const unsigned long long m2 = m * m;  // [2^46, 2^48)
+  const int c2 = (int)(m2 >> 47);       // m^2 >= 2^47: one more binade
+  u = __longlong_as_double(((long long)(2 * E + c2 + 1023) << 52) | ((m2 << (6 - c2)) & 0xFFFFFFFFFFFFFull));
+  // m^3 / 2^16 = (m2_hi m) 2^16 + (m2_lo m) / 2^16, in [2^53, 2^56)
+  const unsigned long long t = (((m2 >> 32) * m) << 16) + (((m2 & 0xFFFFFFFFull) * m) >> 16);
+  const int p = 63 - __clzll((long long)t);  // 53, 54 or 55
+  y3 = __longlong_as_double(((long long)(3 * E + p - 53 + 1023) << 52) | ((t >> (p - 52)) & 0xFFFFFFFFFFFFFull));
+}
+
+// 1 + 15/8 e^2 in FP64 from e's high word: for the Newton residual (|e| <
+// 2^-20) the term is below 2^-37 and is needed to 2^-53, i.e. to 16 of its
+// own bits, which FP32 gives; it is placed in the low bits of 1.0 by an
+// integer addition.  Larger |e| (only the sink's own pair, r^2 = 0, whose
+// displacement is 0) is clamped so that the result stays finite.
+__device__ __forceinline__ double one_plus_q(double e) {
+  const int eh = __double2hiint(e);
+  const int ex = (eh >> 20) & 0x7FF;
+  const int fx = min(ex, 0x47E) - 0x380;  // float exponent field of |e|
+  const float ef = fx > 0 ? __int_as_float((fx << 23) | ((eh & 0xFFFFF) << 3)) : 0.0f;
+  const float q = fminf(1.875f * ef * ef, 4.656612873077393e-10f);  // <= 2^-31
+  const float t = __fmaf_rn(q, 4503599627370496.0f, 12582912.0f);  // q 2^52 + 1.5 2^23: rounds to an integer
+  return __longlong_as_double(0x3FF0000000000000LL + (long long)(__float_as_int(t) - 0x4B400000));
+}
+
 // Split pair arithmetic: FP64 displacement and r^2; rsqrt seed in FP32 with
 // the FP64 <-> FP32 conversions done by integer operations on the bit
 // patterns (they stay off the FP64 pipe); one FP64 Newton correction of
 // r^-3 carried to second order in the residual e = 1 - r^2 y0^2:
 //   r^-3 = y0^3 (1 - e)^(-3/2) = y0^3 (1 + 3/2 e + 15/8 e^2 + O(e^3)),
-// |e| < 1e-6, so the truncation is below 1e-18.  16 FP64 operations per pair.
+// |e| < 2^-20, so the truncation is below 1e-18.  The seed's square and cube
+// come from the integer pipe (seed_square_cube) and 1 + 15/8 e^2 from FP32
+// (one_plus_q), leaving FP64 the residual, the correction 3/2 e + (1 + 15/8
+// e^2) by one DFMA and G m y0^3 corr (split_gm_rinv3): with the displacement,
+// r^2 and the three accumulations, 13 FP64 operations per pair.
+__device__ __forceinline__ double split_gm_rinv3(double r2, double gm) {
+  // FP64 -> FP32 by truncation of the high word, clamped to the normal FP32
+  // range so that r2 == 0 (the sink itself) gives a finite seed.
+  int hi = __double2hiint(r2);
+  hi = min(max(hi, 0x38100000), 0x47EFFFFF);
+  const float f = __int_as_float((hi - 0x38000000) << 3);
+  double u, y3;
+  seed_square_cube(rsqrtf(f), u, y3);
+  const double e = __fma_rn(-r2, u, 1.0);
+  const double corr = __fma_rn(1.5, e, one_plus_q(e));
+  return (gm * y3) * corr;
+}
+
 __device__ __forceinline__ void pair_split(const TileSmem<4>& sm, int st, int jj, int j, int i, int ns, double xi,
                                            double yi, double zi, double& ax, double& ay, double& az,
                                            long long& r2minb, int& nn) {
@@ -230,21 +279,8 @@ __device__ __forceinline__ void pair_split(const TileSmem<4>& sm, int st, int jj
   double dy = sm.v[st][SY][jj] - yi;
   double dz = sm.v[st][SZ][jj] - zi;
   double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, dz * dz));
-  // FP64 -> FP32 by truncation of the high word, clamped to the normal FP32
-  // range so that r2 == 0 (the sink itself) gives a finite seed.
-  int hi = __double2hiint(r2);
-  hi = min(max(hi, 0x38100000), 0x47EFFFFF);
-  float f = __int_as_float((hi - 0x38000000) << 3);
-  float yf = rsqrtf(f);
-  int fb = __float_as_int(yf);
-  double y0 = __hiloint2double((fb >> 3) + 0x38000000, fb << 29);
-  double u = y0 * y0;
-  double e = __fma_rn(-r2, u, 1.0);
-  double y3 = u * y0;
-  double cpoly = __fma_rn(e, 1.875, 1.5);
-  double corr = __fma_rn(e, cpoly, 1.0);
   double gm = (j < ns) ? sm.v[st][SGM][jj] : 0.0;  // gm of j == 0 and of padding is 0
-  double s = (gm * y3) * corr;
+  double s = split_gm_rinv3(r2, gm);
   ax = __fma_rn(s, dx, ax);
   ay = __fma_rn(s, dy, ay);
   az = __fma_rn(s, dz, az);
@@ -1235,17 +1271,8 @@ __global__ void __launch_bounds__(kFewSplitWarps * 32) k_pairs_few(ForceCtx fc, 
     for (int j = lane; j < ns; j += 32) {
       const double dx = sx[j] - xi, dy = sy[j] - yi, dz = sz[j] - zi;
       const double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, dz * dz));
-      int hi = __double2hiint(r2);
-      hi = min(max(hi, 0x38100000), 0x47EFFFFF);
-      const float f = __int_as_float((hi - 0x38000000) << 3);
-      const int fb = __float_as_int(rsqrtf(f));
-      const double y0 = __hiloint2double((fb >> 3) + 0x38000000, fb << 29);
-      const double u = y0 * y0;
-      const double e = __fma_rn(-r2, u, 1.0);
-      const double y3 = u * y0;
-      const double corr = __fma_rn(e, __fma_rn(e, 1.875, 1.5), 1.0);
       const double gm = (j >= 1 && j != i) ? sg[j] : 0.0;  // the sink itself and the central body: 0
-      const double sc = (gm * y3) * corr;
+      const double sc = split_gm_rinv3(r2, gm);
       ax = __fma_rn(sc, dx, ax);
       ay = __fma_rn(sc, dy, ay);
       az = __fma_rn(sc, dz, az);
