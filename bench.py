@@ -162,7 +162,7 @@ def _figures(p):
     return out
 
 
-FF_FP32_OPS_PER_PAIR = 116
+FF_FP32_OPS_PER_PAIR = 111
 # The FP32 pipe completes 128 lane operations per SM cycle (4 sub-partitions x
 # 32 lanes; a paired FFMA2 instruction is two).
 FP32_LANES_PER_SM_CYCLE = 128.0
@@ -635,7 +635,7 @@ def main():
     fp64_ops = {"split_ff": 0, "split": 13, "fp64": 17}
     # SPLIT_FF's pair (k_pairs_ff) runs on the FP32 pipe: FP32 lane operations
     # per pair of its float-float arithmetic (sol_pair.cuh): the displacement
-    # from the grid triples 21, r^2 25, G m r^-3 25, the accumulation 45
+    # from the grid triples 21, r^2 23, G m r^-3 22, the accumulation 45
     fp32_ops = {"split_ff": FF_FP32_OPS_PER_PAIR}
     prof = profile_figures()
 

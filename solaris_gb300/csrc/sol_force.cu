@@ -989,10 +989,11 @@ __device__ __forceinline__ void ff_nn(float r2h, float r2l, bool ok, int j, floa
   nn = better ? j : nn;
 }
 
-// Two sources (j, j + 1) of the tile against the sink.  MASKED: per-pair
-// validity (source range, the sink itself, the chunk end) is tested.
+// Two sources (j, j + 1) of the tile against the sink, their table rows in
+// sv (one float2 per row).  MASKED: per-pair validity (source range, the
+// sink itself, the chunk end) is tested.
 template <bool MASKED>
-__device__ __forceinline__ void ff_two_sources(const FFTile& sm, int st, int jj, int j, int i, int ns, int jend,
+__device__ __forceinline__ void ff_two_sources(const float2* sv, int j, int i, int ns, int jend,
                                                const float* ai, const float* bi, const float* ci, float thr,
                                                const ForceCtx& fc, double xi, double yi, double zi, float2* Ah,
                                                float2* Al, double& fx, double& fy, double& fz, float& mh, float& ml,
@@ -1000,11 +1001,9 @@ __device__ __forceinline__ void ff_two_sources(const FFTile& sm, int st, int jj,
   float2 h[3], l[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k)
-    f2_grid_disp(*reinterpret_cast<const float2*>(&sm.v[st][FAX + 3 * k][jj]),
-                 *reinterpret_cast<const float2*>(&sm.v[st][FBX + 3 * k][jj]),
-                 *reinterpret_cast<const float2*>(&sm.v[st][FCX + 3 * k][jj]), ai[k], bi[k], ci[k], h[k], l[k]);
-  float2 gh = *reinterpret_cast<const float2*>(&sm.v[st][FGH][jj]);
-  float2 gl = *reinterpret_cast<const float2*>(&sm.v[st][FGL][jj]);
+    f2_grid_disp(sv[FAX + 3 * k], sv[FBX + 3 * k], sv[FCX + 3 * k], ai[k], bi[k], ci[k], h[k], l[k]);
+  float2 gh = sv[FGH];
+  float2 gl = sv[FGL];
   float2 r2h, r2l;
   f2_ff_r2(h, l, r2h, r2l);
   bool ok0 = true, ok1 = true;
@@ -1102,14 +1101,29 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs_ff(ForceCtx fc, const doub
 #pragma unroll
       for (int k = 0; k < 3; ++k) Ah[k] = Al[k] = make_float2(0.0f, 0.0f);
       if (fast) {
-#pragma unroll 2
-        for (int jj = 0; jj < kTile; jj += 2)
-          ff_two_sources<false>(sm, st, jj, j0 + jj, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy,
-                                fz, mh, ml, nn);
+        // four sources per step: one 16-byte shared load per table row
+#pragma unroll 1
+        for (int jj = 0; jj < kTile; jj += 4) {
+          float2 va[kFF], vb[kFF];
+#pragma unroll
+          for (int k = 0; k < kFF; ++k) {
+            const float4 q = *reinterpret_cast<const float4*>(&sm.v[st][k][jj]);
+            va[k] = make_float2(q.x, q.y);
+            vb[k] = make_float2(q.z, q.w);
+          }
+          ff_two_sources<false>(va, j0 + jj, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy, fz, mh,
+                                ml, nn);
+          ff_two_sources<false>(vb, j0 + jj + 2, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy, fz,
+                                mh, ml, nn);
+        }
       } else {
-        for (int jj = 0; jj < jend - j0; jj += 2)
-          ff_two_sources<true>(sm, st, jj, j0 + jj, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy,
-                               fz, mh, ml, nn);
+        for (int jj = 0; jj < jend - j0; jj += 2) {
+          float2 va[kFF];
+#pragma unroll
+          for (int k = 0; k < kFF; ++k) va[k] = *reinterpret_cast<const float2*>(&sm.v[st][k][jj]);
+          ff_two_sources<true>(va, j0 + jj, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy, fz, mh, ml,
+                               nn);
+        }
       }
       // the tile's float-float partials (even and odd sources) into the FP64 chunk sums
       two_sum(ax, cx, ((double)Ah[0].x + (double)Al[0].x) + ((double)Ah[0].y + (double)Al[0].y));
@@ -1377,18 +1391,22 @@ __global__ void __launch_bounds__(kFewSplitWarps * 32) k_pairs_few(ForceCtx fc, 
 // parts: 1 = prepass (and indirect totals), 2 = pair kernel, 3 = both.
 // Sources per CTA of the 2-D split kernels: SPLIT takes kChunk; SPLIT_FF a
 // chunk of 1..kChunkTiles tiles: among the grids that give every SM at least
-// the four CTAs k_pairs_ff holds, the one whose busiest SM has the least
+// the CTAs k_pairs_ff holds at once, the one whose busiest SM has the least
 // work (its CTAs times the tiles of a CTA plus half a tile of per-CTA work),
 // ties to the larger chunk; the finest chunk when no grid is that large.
 // Small systems fill the GPU, and sizes just past a whole number of CTAs
 // per SM avoid a nearly empty last round.
 static int split_chunk(const sol_ctx* c, int precision) {
   if (precision != SOL_PRECISION_SPLIT_FF) return kChunk;
-  static int sms[kMaxDevices];
+  static int sms[kMaxDevices], resident[kMaxDevices];
   const int dev = (c->device >= 0 && c->device < kMaxDevices) ? c->device : 0;
   if (sms[dev] == 0) {
-    int nsm = 0;
+    int nsm = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 152;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_ff, kSinkBlock, 0) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 3;
+    resident[dev] = per_sm;
     sms[dev] = nsm;
   }
   const long nb = (c->n + kSinkBlock - 1) / kSinkBlock;
@@ -1397,7 +1415,7 @@ static int split_chunk(const sol_ctx* c, int precision) {
   double best = 1e300;
   for (int ct = kChunkTiles; ct >= 1; ct >>= 1) {
     const long ctas = nb * ((c->n + ct * kTile - 1) / (ct * kTile));
-    if (ctas < 4 * nsm) continue;
+    if (ctas < (long)resident[dev] * nsm) continue;
     const double cost = (double)((ctas + nsm - 1) / nsm) * (ct + 0.5);
     if (cost < best) {
       best = cost;

@@ -173,8 +173,8 @@ __device__ __forceinline__ void f2_two_sum_pos(float2 a, float2 b, float2& s, fl
 }
 
 // r^2 = sum_k (h_k + l_k)^2 as a float-float (exact squares of the high
-// words, TwoSum of the three non-negative squares, the cross terms 2 h l
-// and the squares' errors in the low word).
+// words, TwoSum of the three non-negative squares, the cross terms
+// 2 sum_k h_k l_k and the squares' errors in the low word).
 __device__ __forceinline__ void f2_ff_r2(const float2* h, const float2* l, float2& r2h, float2& r2l) {
   float2 p[3], e[3];
 #pragma unroll
@@ -183,14 +183,18 @@ __device__ __forceinline__ void f2_ff_r2(const float2* h, const float2* l, float
   f2_two_sum_pos(p[0], p[1], s12, t12);
   f2_two_sum_pos(s12, p[2], s3, t3);
   float2 lo = f2_add(f2_add(t12, t3), f2_add(f2_add(e[0], e[1]), e[2]));
-#pragma unroll
-  for (int k = 0; k < 3; ++k) lo = f2_fma(f2_add(h[k], h[k]), l[k], lo);
+  const float2 cross = f2_fma(h[0], l[0], f2_fma(h[1], l[1], f2_mul(h[2], l[2])));
+  lo = f2_fma(f2_splat(2.0f), cross, lo);
   f2_fast_two_sum(s3, lo, r2h, r2l);
 }
 
 // G m r^-3 as a float-float from r^2 = (qh, ql): the FP32 rsqrt seed y, the
 // residual e = 1 - r^2 y^2 from exact products, r^-3 = y^3 (1 + 3/2 e +
-// 15/8 e^2) (|e| < 2^-21: truncation ~2^-60), times G m = (gh, gl).
+// 15/8 e^2) (|e| < 2^-21: truncation ~2^-60), times G m = (gh, gl).  The
+// product is left unnormalised: its low word, the TwoProduct error and the
+// two cross terms, stays within 3 2^-24 of the high word, and the
+// accumulation that takes it multiplies it by the displacement with one
+// rounding (f2_ff_accumulate).
 __device__ __forceinline__ void f2_ff_gm_rinv3(float2 qh, float2 ql, float2 gh, float2 gl, float2& sh, float2& se) {
   const float2 y = make_float2(rsqrtf(qh.x), rsqrtf(qh.y));
   float2 y2, y2e, q, qe;
@@ -205,11 +209,10 @@ __device__ __forceinline__ void f2_ff_gm_rinv3(float2 qh, float2 ql, float2 gh, 
   f2_fast_two_sum(y3h, f2_fma(y3h, c, y3e), Rh, Rl);
   f2_two_prod(gh, Rh, sh, se);
   se = f2_fma(gh, Rl, f2_fma(gl, Rh, se));
-  f2_fast_two_sum(sh, se, sh, se);
 }
 
-// A += s d for one component, float-float (s and d float-float, A kept
-// normalised).
+// A += s d for one component, float-float (s and d float-float, |s_lo| <=
+// 3 2^-24 |s_hi|; A kept normalised).
 __device__ __forceinline__ void f2_ff_accumulate(float2& Ah, float2& Al, float2 sh, float2 se, float2 dh, float2 dl) {
   float2 ah, ae;
   f2_two_prod(sh, dh, ah, ae);
