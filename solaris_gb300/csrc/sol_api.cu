@@ -17,7 +17,7 @@ int sol_force_prepass_blocks(int npad);
 int sol_force_src_doubles();
 int sol_force_launch_sinks(sol_ctx* c, const double* d_y, double* d_dydt, TimeSpec ts, uint32_t flags, int lo, int hi);
 int sol_integrate_partials_needed(int nv);
-int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_pe);
+int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_part, int* nparts);
 
 // ---- errors and counters -----------------------------------------------------
 static thread_local char g_err[1024] = "";
@@ -815,11 +815,13 @@ int sol_integrals(sol_ctx* c, const double* y0_or_null, double o[16]) {
   // Calculate::PotentialEnergy (Calculate.cpp:139-159) adds every ordered
   // pair into one running sum.  Up to kExactPotentialMax bodies (scenario
   // sizes, ~1 M pairs at most) that sum runs here in the reference's order,
-  // bit for bit; above, the device sums per body and the host sums those.
+  // bit for bit; above, the device sums each unordered pair once into
+  // per-CTA partials (k_potential_pairs) and the host adds those in order.
   const bool exact_order = N <= kExactPotentialMax;
+  int nparts = 0;
   if (!exact_order) {
-    RET(sol_potential_launch(c, d_y, c->d_io_out));
-    SOL_CUDA(cudaMemcpyAsync(pe.data(), c->d_io_out, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    RET(sol_potential_launch(c, d_y, c->d_io_out, &nparts));
+    SOL_CUDA(cudaMemcpyAsync(pe.data(), c->d_io_out, sizeof(double) * nparts, cudaMemcpyDeviceToHost, c->stream));
   }
   SOL_CUDA(cudaMemcpyAsync(y.data(), d_y, sizeof(double) * c->nv, cudaMemcpyDeviceToHost, c->stream));
   SOL_CUDA(cudaMemcpyAsync(mass.data(), c->d_mass, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
@@ -868,7 +870,9 @@ int sol_integrals(sol_ctx* c, const double* y0_or_null, double o[16]) {
       }
     }
   } else {
-    for (int i = 0; i < N; i++) pes += pe[i];
+    double unordered = 0.0;
+    for (int b = 0; b < nparts; b++) unordered += pe[b];
+    pes = 2.0 * unordered;
   }
   o[14] = pes * (0.5 * 2.959122082855911025e-4);
   o[15] = o[13] - o[14];

@@ -40,13 +40,32 @@ __global__ void k_events(int n, const double* __restrict__ rm3, const int32_t* _
   }
 }
 
-// Per-body potential-energy sums of Calculate::PotentialEnergy
-// (Solaris/Calculate.cpp:139-159): pe[i] = sum_{j != i} m_i m_j / r_ij, sources
-// staged through shared memory; the host finishes the O(N) parts.
-__global__ void k_potential(int n, const double* __restrict__ y0, const double* __restrict__ mass,
-                            double* __restrict__ pe) {
-  __shared__ double sx[kBlock], sy[kBlock], sz[kBlock], sm[kBlock];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Calculate::PotentialEnergy (Solaris/Calculate.cpp:139-159) above the
+// exact-order size: the sum over unordered pairs of m_i m_j / r_ij, each
+// pair evaluated once (the reference adds every ordered pair, i.e. each
+// unordered pair twice, and halves the total).  CTA b takes the sink block
+// I = b and the source blocks (I + d) mod nb for d = 0 .. nb/2, except that
+// for an even nb the block at distance nb/2 goes to the lower half only:
+// every unordered block pair once, every CTA about nb/2 blocks.  The block
+// itself (d = 0) takes j > i.  1/r_ij is the FP32 rsqrt seed y corrected in
+// FP64 by r^-1 = y (1 + e/2 + 3/8 e^2), e = 1 - r^2 y^2 (|e| < 2^-20, series
+// truncation ~2^-65): y and y^2 exact from the seed's bits, 3/8 e^2 in FP32,
+// so a pair costs 10 FP64 instructions (against ~23 with IEEE sqrt and
+// division).  Coincident bodies (r_ij = 0) add m_j inf, scaled by m_i at the
+// end: +inf, or NaN where either mass is 0, as the reference's
+// m_i m_j / 0 gives.  Each thread sums its sink's terms per block with a
+// compensated running sum, scales by m_i, and the CTA adds its threads' sums
+// in thread order: part[b], deterministic.
+constexpr int kPotBlock = 128;
+
+__global__ void __launch_bounds__(kPotBlock) k_potential_pairs(int n, const double* __restrict__ y0,
+                                                               const double* __restrict__ mass,
+                                                               double* __restrict__ part) {
+  __shared__ double sx[kPotBlock], sy[kPotBlock], sz[kPotBlock], sm[kPotBlock];
+  __shared__ double red[kPotBlock];
+  const int nb = (n + kPotBlock - 1) / kPotBlock;
+  const int I = blockIdx.x;
+  const int i = I * kPotBlock + threadIdx.x;
   double xi = 0, yi = 0, zi = 0, mi = 0;
   if (i < n) {
     xi = y0[6 * i];
@@ -54,9 +73,12 @@ __global__ void k_potential(int n, const double* __restrict__ y0, const double* 
     zi = y0[6 * i + 2];
     mi = mass[i];
   }
-  double acc = 0.0;
-  for (int j0 = 0; j0 < n; j0 += kBlock) {
-    int j = j0 + threadIdx.x;
+  const int dmax = (nb % 2 == 0 && I >= nb / 2) ? nb / 2 - 1 : nb / 2;
+  double s = 0.0, c = 0.0;
+  for (int d = 0; d <= dmax; ++d) {
+    const int J = (I + d) % nb;
+    const int j = J * kPotBlock + threadIdx.x;
+    __syncthreads();
     if (j < n) {
       sx[threadIdx.x] = y0[6 * j];
       sy[threadIdx.x] = y0[6 * j + 1];
@@ -64,17 +86,34 @@ __global__ void k_potential(int n, const double* __restrict__ y0, const double* 
       sm[threadIdx.x] = mass[j];
     }
     __syncthreads();
-    const int lim = min(kBlock, n - j0);
+    const int lim = min(kPotBlock, n - J * kPotBlock);
+    const int q0 = d == 0 ? threadIdx.x + 1 : 0;  // the block itself: j > i
+    double acc = 0.0;
     if (i < n)
-      for (int q = 0; q < lim; ++q) {
-        if (j0 + q == i) continue;
-        double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
-        double rij = __dsqrt_rn(dx * dx + dy * dy + dz * dz);
-        acc += __ddiv_rn(mi * sm[q], rij);
+      for (int q = q0; q < lim; ++q) {
+        const double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
+        const double r2 = __fma_rn(dx, dx, __fma_rn(dy, dy, dz * dz));
+        const float yf = sol_rsqrt_seed(r2);
+        const double e = __fma_rn(-r2, sol_seed_square(yf), 1.0);
+        const double corr = __fma_rn(0.5, e, sol_one_plus_ce2(e, 0.375f));
+        const double t = sm[q] * sol_seed_double(yf);
+        acc = r2 > 0.0 ? __fma_rn(t, corr, acc) : acc + sm[q] * __longlong_as_double(0x7FF0000000000000LL);
       }
-    __syncthreads();
+    // compensated running sum of the blocks (Knuth's TwoSum) while it is finite
+    const double u = s + acc;
+    if (isfinite(u)) {
+      const double bp = u - s;
+      c += (s - (u - bp)) + (acc - bp);
+    }
+    s = u;
   }
-  if (i < n) pe[i] = acc;
+  red[threadIdx.x] = i < n ? mi * (s + c) : 0.0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < kPotBlock; ++k) t += red[k];
+    part[I] = t;
+  }
 }
 
 // FP64 pipe throughput: kRateChains independent chains of one FP64
@@ -309,9 +348,10 @@ int sol_events_launch(sol_ctx* c, const double* d_y0, double ej, double hc, doub
   return SOL_OK;
 }
 
-int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_pe) {
-  int g = (c->n + kBlock - 1) / kBlock;
-  k_potential<<<g, kBlock, 0, c->stream>>>(c->n, d_y0, c->d_mass, d_pe);
+int sol_potential_launch(sol_ctx* c, const double* d_y0, double* d_part, int* nparts) {
+  const int g = (c->n + kPotBlock - 1) / kPotBlock;
+  k_potential_pairs<<<g, kPotBlock, 0, c->stream>>>(c->n, d_y0, c->d_mass, d_part);
+  *nparts = g;
   SOL_LAUNCHED();
   return SOL_OK;
 }

@@ -217,58 +217,22 @@ __device__ __forceinline__ void pair_fp64(const TileSmem<7>& sm, int st, int jj,
   }
 }
 
-// The FP32 seed y (positive, normal) as y^2 and y^3 in FP64 without FP64
-// instructions: from y's 24-bit significand m by integer multiplies, y^2 =
-// m^2 (48 bits, exact) and y^3 = m^3 (72 bits, truncated to 53), with the
-// exponents set directly.
-__device__ __forceinline__ void seed_square_cube(float yf, double& u, double& y3) {
-  const unsigned b = __float_as_uint(yf);
-  const int E = (int)(b >> 23) - 127;  // yf = 2^E m 2^-23
-  const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
-  const unsigned long long m2 = m * m;  // [2^46, 2^48)
-  const int c2 = (int)(m2 >> 47);       // m^2 >= 2^47: one more binade
-  u = __longlong_as_double(((long long)(2 * E + c2 + 1023) << 52) | ((m2 << (6 - c2)) & 0xFFFFFFFFFFFFFull));
-  // m^3 / 2^16 = (m2_hi m) 2^16 + (m2_lo m) / 2^16, in [2^53, 2^56)
-  const unsigned long long t = (((m2 >> 32) * m) << 16) + (((m2 & 0xFFFFFFFFull) * m) >> 16);
-  const int p = 63 - __clzll((long long)t);  // 53, 54 or 55
-  y3 = __longlong_as_double(((long long)(3 * E + p - 53 + 1023) << 52) | ((t >> (p - 52)) & 0xFFFFFFFFFFFFFull));
-}
-
-// 1 + 15/8 e^2 in FP64 from e's high word: for the Newton residual (|e| <
-// 2^-20) the term is below 2^-37 and is needed to 2^-53, i.e. to 16 of its
-// own bits, which FP32 gives; it is placed in the low bits of 1.0 by an
-// integer addition.  Larger |e| (only the sink's own pair, r^2 = 0, whose
-// displacement is 0) is clamped so that the result stays finite.
-__device__ __forceinline__ double one_plus_q(double e) {
-  const int eh = __double2hiint(e);
-  const int ex = (eh >> 20) & 0x7FF;
-  const int fx = min(ex, 0x47E) - 0x380;  // float exponent field of |e|
-  const float ef = fx > 0 ? __int_as_float((fx << 23) | ((eh & 0xFFFFF) << 3)) : 0.0f;
-  const float q = fminf(1.875f * ef * ef, 4.656612873077393e-10f);  // <= 2^-31
-  const float t = __fmaf_rn(q, 4503599627370496.0f, 12582912.0f);  // q 2^52 + 1.5 2^23: rounds to an integer
-  return __longlong_as_double(0x3FF0000000000000LL + (long long)(__float_as_int(t) - 0x4B400000));
-}
-
 // Split pair arithmetic: FP64 displacement and r^2; rsqrt seed in FP32 with
 // the FP64 <-> FP32 conversions done by integer operations on the bit
 // patterns (they stay off the FP64 pipe); one FP64 Newton correction of
 // r^-3 carried to second order in the residual e = 1 - r^2 y0^2:
 //   r^-3 = y0^3 (1 - e)^(-3/2) = y0^3 (1 + 3/2 e + 15/8 e^2 + O(e^3)),
 // |e| < 2^-20, so the truncation is below 1e-18.  The seed's square and cube
-// come from the integer pipe (seed_square_cube) and 1 + 15/8 e^2 from FP32
-// (one_plus_q), leaving FP64 the residual, the correction 3/2 e + (1 + 15/8
+// come from the integer pipe (sol_seed_square_cube) and 1 + 15/8 e^2 from
+// FP32 (sol_one_plus_ce2), leaving FP64 the residual, the correction 3/2 e + (1 + 15/8
 // e^2) by one DFMA and G m y0^3 corr (split_gm_rinv3): with the displacement,
 // r^2 and the three accumulations, 13 FP64 operations per pair.
 __device__ __forceinline__ double split_gm_rinv3(double r2, double gm) {
-  // FP64 -> FP32 by truncation of the high word, clamped to the normal FP32
-  // range so that r2 == 0 (the sink itself) gives a finite seed.
-  int hi = __double2hiint(r2);
-  hi = min(max(hi, 0x38100000), 0x47EFFFFF);
-  const float f = __int_as_float((hi - 0x38000000) << 3);
+  // the seed of r2 == 0 (the sink itself) is finite
   double u, y3;
-  seed_square_cube(rsqrtf(f), u, y3);
+  sol_seed_square_cube(sol_rsqrt_seed(r2), u, y3);
   const double e = __fma_rn(-r2, u, 1.0);
-  const double corr = __fma_rn(1.5, e, one_plus_q(e));
+  const double corr = __fma_rn(1.5, e, sol_one_plus_ce2(e, 1.875f));
   return (gm * y3) * corr;
 }
 

@@ -108,6 +108,59 @@ __device__ __forceinline__ void ff_pair_accumulate(double dxd, double dyd, doubl
   r2l_out = r2l;
 }
 
+// ---- FP32 seed, FP64 Newton step: the pieces that stay off the FP64 pipe ----
+// The FP32 seed y (positive, normal) as a double (exact), y^2 and y^3 in FP64
+// without FP64 instructions: from y's 24-bit significand m by integer
+// multiplies, y^2 = m^2 (48 bits, exact) and y^3 = m^3 (72 bits, truncated to
+// 53), with the exponents set directly.
+__device__ __forceinline__ double sol_seed_double(float yf) {
+  const int b = __float_as_int(yf);
+  return __hiloint2double((b >> 3) + 0x38000000, b << 29);
+}
+__device__ __forceinline__ void sol_seed_square_cube(float yf, double& u, double& y3) {
+  const unsigned b = __float_as_uint(yf);
+  const int E = (int)(b >> 23) - 127;  // yf = 2^E m 2^-23
+  const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
+  const unsigned long long m2 = m * m;  // [2^46, 2^48)
+  const int c2 = (int)(m2 >> 47);       // m^2 >= 2^47: one more binade
+  u = __longlong_as_double(((long long)(2 * E + c2 + 1023) << 52) | ((m2 << (6 - c2)) & 0xFFFFFFFFFFFFFull));
+  // m^3 / 2^16 = (m2_hi m) 2^16 + (m2_lo m) / 2^16, in [2^53, 2^56)
+  const unsigned long long t = (((m2 >> 32) * m) << 16) + (((m2 & 0xFFFFFFFFull) * m) >> 16);
+  const int p = 63 - __clzll((long long)t);  // 53, 54 or 55
+  y3 = __longlong_as_double(((long long)(3 * E + p - 53 + 1023) << 52) | ((t >> (p - 52)) & 0xFFFFFFFFFFFFFull));
+}
+__device__ __forceinline__ double sol_seed_square(float yf) {
+  const unsigned b = __float_as_uint(yf);
+  const int E = (int)(b >> 23) - 127;
+  const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
+  const unsigned long long m2 = m * m;
+  const int c2 = (int)(m2 >> 47);
+  return __longlong_as_double(((long long)(2 * E + c2 + 1023) << 52) | ((m2 << (6 - c2)) & 0xFFFFFFFFFFFFFull));
+}
+
+// 1 + c e^2 in FP64 (0 <= c <= 2) from e's high word: for a Newton residual
+// (|e| < 2^-20) the term is below 2^-37 and is needed to 2^-53, i.e. to 16 of
+// its own bits, which FP32 gives; it is placed in the low bits of 1.0 by an
+// integer addition.  Larger |e| (only a pair at r^2 = 0, whose seed is
+// clamped) is clamped so that the result stays finite.
+__device__ __forceinline__ double sol_one_plus_ce2(double e, float c) {
+  const int eh = __double2hiint(e);
+  const int ex = (eh >> 20) & 0x7FF;
+  const int fx = min(ex, 0x47E) - 0x380;  // float exponent field of |e|
+  const float ef = fx > 0 ? __int_as_float((fx << 23) | ((eh & 0xFFFFF) << 3)) : 0.0f;
+  const float q = fminf(c * ef * ef, 4.656612873077393e-10f);  // <= 2^-31
+  const float t = __fmaf_rn(q, 4503599627370496.0f, 12582912.0f);  // q 2^52 + 1.5 2^23: rounds to an integer
+  return __longlong_as_double(0x3FF0000000000000LL + (long long)(__float_as_int(t) - 0x4B400000));
+}
+
+// FP64 r^2 -> FP32 by truncation of the high word, clamped to the normal FP32
+// range (r^2 == 0 gives a finite seed), and its rsqrt seed.
+__device__ __forceinline__ float sol_rsqrt_seed(double r2) {
+  int hi = __double2hiint(r2);
+  hi = min(max(hi, 0x38100000), 0x47EFFFFF);
+  return rsqrtf(__int_as_float((hi - 0x38000000) << 3));
+}
+
 // ---- paired FP32 (f32x2): one instruction computes two lanes ----------------
 // Blackwell's paired FP32 arithmetic (add / sub / mul / fma .f32x2, round to
 // nearest even per lane) halves the instruction count of float-float code
