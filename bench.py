@@ -670,7 +670,10 @@ def main():
                        "fp32_ops_per_pair": fp32_ops.get(name),
                        "fp32_pipe_frac": pps * fp32_ops[name] / peak32 if name in fp32_ops else None,
                        "conventional_tflops": pps * FLOP_PER_PAIR / 1e12,
-                       "conventional_frac_of_fp64_peak": pps * FLOP_PER_PAIR / (2.0 * peak_ops),
+                       # the conventional count against the FP64 peak means something only for the
+                       # forms whose pair runs on the FP64 pipe; SPLIT_FF's runs on the FP32 pipe
+                       "conventional_frac_of_fp64_peak": (pps * FLOP_PER_PAIR / (2.0 * peak_ops)
+                                                          if fp64_ops[name] else None),
                        "energy_drift": r["energy_drift"], "steps": r.get("k")}
         if name in acc:
             forms[name]["max_rel_accel_err"], forms[name]["rms_rel_accel_err"] = acc[name]
