@@ -138,7 +138,7 @@ __device__ __forceinline__ bool sol_ref_rinv3_fast(double a, double& rij, double
   const float mh = __uint_as_float(((unsigned)(127 + p) << 23) | ((hiA & 0x000FFFFFu) << 3) | (loA >> 29));
   const float ml = __uint2float_rn(loA & 0x1FFFFFFFu) * __uint_as_float((unsigned)(127 + p - 52) << 23);
   // seed and residual e = 1 - m y^2 from exact products
-  const float y = rsqrtf(mh);
+  const float y = sol_rsqrt_normal(mh);  // mh in [1, 4)
   float y2, y2e, q, qe;
   ff_two_prod(y, y, y2, y2e);
   ff_two_prod(mh, y2, q, qe);

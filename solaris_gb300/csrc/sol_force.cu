@@ -1027,7 +1027,9 @@ __global__ void __launch_bounds__(kSinkBlock) k_pairs_ff(ForceCtx fc, const doub
     zi = y[6 * i + 2];
   }
   const double G1 = fc.ind_sum[kIndGrid];
-  const float thr = (float)(G1 * G1);  // |d| < G1: the FP64 branch
+  // |d| < max(G1, 2^-50): the FP64 branch (the floor keeps every r^2 the
+  // float-float path sees a normal float)
+  const float thr = fmaxf((float)(G1 * G1), 7.888609052210118e-31f);
 
   if (threadIdx.x == 0) {
     sol_mbar_init(&sm.bar[0], 1);
