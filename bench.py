@@ -46,7 +46,56 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_BODIES, help=argparse.SUPPRESS)
     ap.add_argument("--skip-ensemble", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--drift-steps", type=int, default=0,
+                    help="instead of the benchmark line: energy drift of each form over this many RK4 steps")
+    ap.add_argument("--drift-forms", default="split_ff,split,fp64",
+                    help="forms for --drift-steps (comma-separated: split_ff, split, fp64)")
     return ap.parse_args()
+
+
+def run_drift(args, local):
+    """The 65,536-body workload integrated for --drift-steps RK4 steps in each
+    form from the same initial state: the relative energy drift |E - E0| / |E0|
+    (sol_integrals) every tenth of the run, the wall time, and the final state's
+    maximum / RMS relative acceleration error against the FP64 form evaluated
+    at that state.  One JSON line."""
+    import numpy as np
+    import torch
+
+    from solaris_gb300 import abi, build, engine, scenarios
+    build.build()
+    torch.cuda.set_device(local)
+    s = scenarios.config3(n=args.n)
+    forms = {"split_ff": abi.PRECISION_SPLIT_FF, "split": abi.PRECISION_SPLIT, "fp64": abi.PRECISION_FP64}
+    n_steps = args.drift_steps
+    every = max(1, n_steps // 10)
+    out = {"workload": WORKLOAD, "n_bodies": s.n, "integrator": "RungeKutta4", "h": s.h0, "steps": n_steps,
+           "forms": {}}
+    with engine.Context(s, device=local) as ctx:
+        for name in args.drift_forms.split(","):
+            ctx.set_precision(forms[name])
+            ctx.set_state(s.y0)
+            tl = abi.SolTimeLine(0.0, s.h0, 0.0)
+            e0 = ctx.integrals()[15]
+            drift, done = [], 0
+            t0 = time.perf_counter()
+            while done < n_steps:
+                k = min(every, n_steps - done)
+                ctx.driver(abi.RUNGE_KUTTA4, 0, 0, k, time_line=tl)
+                done += k
+                drift.append(abs((ctx.integrals()[15] - e0) / e0))
+            wall = time.perf_counter() - t0
+            y = ctx.get_state()
+            a, *_ = ctx.accel(0.0, y)
+            ctx.set_precision(abi.PRECISION_FP64)
+            a64, *_ = ctx.accel(0.0, y)
+            A, B = a.reshape(-1, 6)[1:, 3:], a64.reshape(-1, 6)[1:, 3:]
+            rel = np.linalg.norm(A - B, axis=1) / np.linalg.norm(B, axis=1)
+            out["forms"][name] = {"relative_energy_drift": drift, "every": every, "wall_s": wall,
+                                  "final_max_rel_accel_err": float(rel.max()),
+                                  "final_rms_rel_accel_err": float(np.sqrt(np.mean(rel ** 2))),
+                                  "final_state_sha": __import__("hashlib").sha256(y.tobytes()).hexdigest()[:16]}
+    print(json.dumps({"drift": out}))
 
 
 # ---- clocks --------------------------------------------------------------------
@@ -547,6 +596,8 @@ def main():
     if world_env > 1 and world_env != args.gpus:
         raise SystemExit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world_env}")
     rank, world, local = replicas.init()
+    if args.drift_steps > 0:
+        return run_drift(args, local)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     if world > 1:

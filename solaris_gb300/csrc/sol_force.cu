@@ -223,17 +223,18 @@ __device__ __forceinline__ void pair_fp64(const TileSmem<7>& sm, int st, int jj,
 // r^-3 carried to second order in the residual e = 1 - r^2 y0^2:
 //   r^-3 = y0^3 (1 - e)^(-3/2) = y0^3 (1 + 3/2 e + 15/8 e^2 + O(e^3)),
 // |e| < 2^-20, so the truncation is below 1e-18.  The seed's square and cube
-// come from the integer pipe (sol_seed_square_cube) and 1 + 15/8 e^2 from
-// FP32 (sol_one_plus_ce2), leaving FP64 the residual, the correction 3/2 e + (1 + 15/8
-// e^2) by one DFMA and G m y0^3 corr (split_gm_rinv3): with the displacement,
-// r^2 and the three accumulations, 13 FP64 operations per pair.
+// come from the integer pipe (sol_seed_square_cube), and so does t = 3/2 e +
+// 15/8 e^2 (sol_split_t), leaving FP64 the residual e, G m y0^3 and
+// G m y0^3 + (G m y0^3) t by one DFMA (split_gm_rinv3): with the
+// displacement, r^2 and the three accumulations, 12 FP64 operations per pair,
+// the floor of this recipe.
 __device__ __forceinline__ double split_gm_rinv3(double r2, double gm) {
   // the seed of r2 == 0 (the sink itself) is finite
   double u, y3;
   sol_seed_square_cube(sol_rsqrt_seed(r2), u, y3);
   const double e = __fma_rn(-r2, u, 1.0);
-  const double corr = __fma_rn(1.5, e, sol_one_plus_ce2(e, 1.875f));
-  return (gm * y3) * corr;
+  const double gy = gm * y3;
+  return __fma_rn(gy, sol_split_t(e), gy);
 }
 
 __device__ __forceinline__ void pair_split(const TileSmem<4>& sm, int st, int jj, int j, int i, int ns, double xi,

@@ -163,6 +163,42 @@ __device__ __forceinline__ double sol_one_plus_ce2(double e, float c) {
   return __longlong_as_double(0x3FF0000000000000LL + (long long)(__float_as_int(t) - 0x4B400000));
 }
 
+// t = 3/2 e + 15/8 e^2 in FP64 without FP64 instructions, for the Newton
+// correction r^-3 = y^3 (1 + t) of a residual e (|e| < 2^-20 for a seed of
+// r^2; e = 1 for r^2 = 0, whose displacement is 0).  3/2 e is 3 M exactly,
+// M e's 53-bit significand, in units of half e's last place; 15/8 e^2
+// (below 2^-37, from e's high word in FP32) is shifted into the same units
+// and added as an integer, and the sum is normalised to 53 bits
+// (truncated): t is needed to 2^-53 absolute, i.e. to ~32 of its own bits,
+// and carries ~2^-52 relative.  No special cases, since a test of e's bits
+// for zero or infinity is turned back into an FP64 comparison by the
+// compiler (measured: one FP64 instruction per pair): e = 0 or subnormal
+// gives |t| < 2^-1020, which leaves y^3 (1 + t) = y^3, and a non-finite e
+// comes with a non-finite displacement that the accumulation carries.
+__device__ __forceinline__ double sol_split_t(double e) {
+  const long long eb = __double_as_longlong(e);
+  const int ex = (int)((eb >> 52) & 0x7FF);
+  const long long M = (eb & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+  long long S = 3 * M;  // 3/2 e in units of 2^(ex - 1076)
+  if (eb < 0) S = -S;
+  // 15/8 e^2 from e's high word (as sol_one_plus_ce2), clamped to 2^-31
+  const int eh = (int)(eb >> 32);
+  const int fx = min(ex, 0x47E) - 0x380;
+  const float ef = fx > 0 ? __int_as_float((fx << 23) | ((eh & 0xFFFFF) << 3)) : 0.0f;
+  const float q = fminf(1.875f * ef * ef, 4.656612873077393e-10f);
+  const int qb = __float_as_int(q);
+  const long long mq = (long long)((qb & 0x7FFFFF) | 0x800000);
+  const int sq = ((qb >> 23) & 0xFF) + 926 - ex;  // q = mq 2^(eq - 150), in units of 2^(ex - 1076)
+  const long long Q = qb == 0 ? 0 : (sq >= 0 ? (mq << min(sq, 38)) : (mq >> min(-sq, 62)));
+  S += Q;
+  const unsigned long long A = (unsigned long long)(S < 0 ? -S : S);
+  const int p = 63 - __clzll((long long)A);  // leading bit (A > 0 when e != 0)
+  const unsigned long long mant = p >= 52 ? (A >> (p - 52)) : (A << (52 - p));
+  const long long bits = ((S < 0 ? 1LL : 0LL) << 63) | ((long long)(p + ex - 53) << 52) |
+                         (long long)(mant & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double(bits);
+}
+
 // FP64 r^2 -> FP32 by truncation of the high word, clamped to the normal FP32
 // range (r^2 == 0 gives a finite seed), and its rsqrt seed.
 __device__ __forceinline__ float sol_rsqrt_seed(double r2) {
