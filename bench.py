@@ -678,12 +678,13 @@ def main():
     peak_ops, peak_info = fp64_peak(local, ff["clocks"])  # FP64 thread instructions per second
     peak32, peak32_info = fp32_peak(local, ff["clocks"])  # FP32 lane operations per second
     # FP64 instructions per pair of each form's arithmetic: SPLIT_FF none (its
-    # pair runs on the FP32 pipe); SPLIT 13 (displacement 3, r^2 3, the Newton
-    # residual and correction 2, G m y^3 corr 2, the accumulation 3; the seed's
-    # square and cube come from the integer pipe); the reference form 14 in the
-    # pair (correctly rounded sqrt and reciprocal by one FMA remainder each,
-    # the six term multiplies on the integer pipe) plus the 3 in-order additions
-    fp64_ops = {"split_ff": 0, "split": 13, "fp64": 17}
+    # pair runs on the FP32 pipe); SPLIT 12 (displacement 3, r^2 3, the Newton
+    # residual 1, G m y^3 and its correction 2, the accumulation 3; the seed's
+    # square and cube and the correction's t come from the integer pipe); the
+    # reference form 14 in the pair (correctly rounded sqrt and reciprocal by
+    # one FMA remainder each, the six term multiplies on the integer pipe) plus
+    # the 3 in-order additions
+    fp64_ops = {"split_ff": 0, "split": 12, "fp64": 17}
     # SPLIT_FF's pair (k_pairs_ff) runs on the FP32 pipe: FP32 lane operations
     # per pair of its float-float arithmetic (sol_pair.cuh): the displacement
     # from the grid triples 21, r^2 23, G m r^-3 22, the accumulation 45
