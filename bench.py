@@ -211,7 +211,7 @@ def _figures(p):
     return out
 
 
-FF_FP32_OPS_PER_PAIR = 111
+FF_FP32_OPS_PER_PAIR = 106.5
 # The FP32 pipe completes 128 lane operations per SM cycle (4 sub-partitions x
 # 32 lanes; a paired FFMA2 instruction is two).
 FP32_LANES_PER_SM_CYCLE = 128.0
@@ -687,7 +687,8 @@ def main():
     fp64_ops = {"split_ff": 0, "split": 12, "fp64": 17}
     # SPLIT_FF's pair (k_pairs_ff) runs on the FP32 pipe: FP32 lane operations
     # per pair of its float-float arithmetic (sol_pair.cuh): the displacement
-    # from the grid triples 21, r^2 23, G m r^-3 22, the accumulation 45
+    # from the grid triples 21, r^2 23, G m r^-3 22, the accumulation 40.5
+    # (12 per component and step, a 3-operation renormalisation every second)
     fp32_ops = {"split_ff": FF_FP32_OPS_PER_PAIR}
     prof = profile_figures()
 

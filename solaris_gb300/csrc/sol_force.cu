@@ -956,9 +956,12 @@ __device__ __forceinline__ void ff_nn(float r2h, float r2l, bool ok, int j, floa
 
 // Two sources (j, j + 1) of the tile against the sink, their table rows in
 // sv (one float2 per row).  MASKED: per-pair validity (source range, the
-// sink itself, the chunk end) is tested.
+// sink itself, the chunk end) is tested.  The accumulators are renormalised
+// when renorm is set: after the second pair of every group of four sources,
+// as ff_four_sources does, so a sink gets the same bits whether its warp
+// takes a tile on the masked path or the fast one.
 template <bool MASKED>
-__device__ __forceinline__ void ff_two_sources(const float2* sv, int j, int i, int ns, int jend,
+__device__ __forceinline__ void ff_two_sources(const float2* sv, int j, int i, int ns, int jend, bool renorm,
                                                const float* ai, const float* bi, const float* ci, float thr,
                                                const ForceCtx& fc, double xi, double yi, double zi, float2* Ah,
                                                float2* Al, double& fx, double& fy, double& fz, float& mh, float& ml,
@@ -992,7 +995,10 @@ __device__ __forceinline__ void ff_two_sources(const float2* sv, int j, int i, i
   float2 sh, se;
   f2_ff_gm_rinv3(qh, ql, gh, gl, sh, se);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) f2_ff_accumulate(Ah[k], Al[k], sh, se, h[k], l[k]);
+  for (int k = 0; k < 3; ++k) {
+    f2_ff_accumulate_lazy(Ah[k], Al[k], sh, se, h[k], l[k]);
+    if (renorm) f2_fast_two_sum(Ah[k], Al[k], Ah[k], Al[k]);
+  }
   ff_nn(r2h.x, r2l.x, ok0, j, mh, ml, nn);
   ff_nn(r2h.y, r2l.y, ok1, j + 1, mh, ml, nn);
 }
@@ -1000,10 +1006,10 @@ __device__ __forceinline__ void ff_two_sources(const float2* sv, int j, int i, i
 
 // Four sources (j .. j + 3) of a fast tile: the displacements and r^2 of both
 // pairs of sources first, one test for a close pair among the four, then
-// G m r^-3 and the accumulation of both in one basic block: the same
-// operations in the same order as two ff_two_sources calls, but the branch
-// no longer splits them into short blocks the scheduler cannot interleave
-// (16.10 -> 14.96 ms at 65,536 bodies).
+// G m r^-3 and the accumulation of both in one basic block, the branch no
+// longer splitting the step into short blocks the scheduler cannot
+// interleave (16.10 -> 14.96 ms at 65,536 bodies); the accumulators are
+// renormalised once per step instead of after each half (14.52 ms).
 __device__ __forceinline__ void ff_close_lane(const ForceCtx& fc, int j, double xi, double yi, double zi, float& gh,
                                               float& gl, double& fx, double& fy, double& fz, float& r2h, float& r2l,
                                               float& qh, float& ql, float thr) {
@@ -1039,9 +1045,11 @@ __device__ __forceinline__ void ff_four_sources(const float2* va, const float2* 
   f2_ff_gm_rinv3(qha, qla, gha, gla, sha, sea);
   f2_ff_gm_rinv3(qhb, qlb, ghb, glb, shb, seb);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) f2_ff_accumulate(Ah[k], Al[k], sha, sea, ha[k], la[k]);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) f2_ff_accumulate(Ah[k], Al[k], shb, seb, hb[k], lb[k]);
+  for (int k = 0; k < 3; ++k) {  // both halves, one renormalisation
+    f2_ff_accumulate_lazy(Ah[k], Al[k], sha, sea, ha[k], la[k]);
+    f2_ff_accumulate_lazy(Ah[k], Al[k], shb, seb, hb[k], lb[k]);
+    f2_fast_two_sum(Ah[k], Al[k], Ah[k], Al[k]);
+  }
   ff_nn(r2ha.x, r2la.x, true, j, mh, ml, nn);
   ff_nn(r2ha.y, r2la.y, true, j + 1, mh, ml, nn);
   ff_nn(r2hb.x, r2lb.x, true, j + 2, mh, ml, nn);
@@ -1138,8 +1146,8 @@ __global__ void __launch_bounds__(kSinkBlock, 3) k_pairs_ff(ForceCtx fc, const d
           float2 va[kFF];
 #pragma unroll
           for (int k = 0; k < kFF; ++k) va[k] = *reinterpret_cast<const float2*>(&sm.v[st][k][jj]);
-          ff_two_sources<true>(va, j0 + jj, i, ns, jend, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx, fy, fz, mh, ml,
-                               nn);
+          ff_two_sources<true>(va, j0 + jj, i, ns, jend, (jj & 2) != 0, ai, bi, ci, thr, fc, xi, yi, zi, Ah, Al, fx,
+                               fy, fz, mh, ml, nn);
         }
       }
       // the tile's float-float partials (even and odd sources) into the FP64 chunk sums

@@ -310,6 +310,22 @@ __device__ __forceinline__ void f2_ff_gm_rinv3(float2 qh, float2 ql, float2 gh, 
   se = f2_fma(gh, Rl, f2_fma(gl, Rh, se));
 }
 
+// A += s d without the final renormalisation: the caller renormalises
+// (FastTwoSum of (Ah, Al)) after every second accumulation, so Al holds at
+// most two steps' errors (|Al| <= ~4 2^-24 |Ah|) and the rounding of its
+// additions stays at ~2^-46 of |A| per step, as with a renormalisation
+// after every step (f2_ff_accumulate), for 3 fewer FP32 operations.
+__device__ __forceinline__ void f2_ff_accumulate_lazy(float2& Ah, float2& Al, float2 sh, float2 se, float2 dh,
+                                                      float2 dl) {
+  float2 ah, ae;
+  f2_two_prod(sh, dh, ah, ae);
+  ae = f2_fma(sh, dl, f2_fma(se, dh, ae));
+  float2 s1, s2;
+  f2_two_sum(Ah, ah, s1, s2);
+  Ah = s1;
+  Al = f2_add(Al, f2_add(s2, ae));
+}
+
 // A += s d for one component, float-float (s and d float-float, |s_lo| <=
 // 3 2^-24 |s_hi|; A kept normalised).
 __device__ __forceinline__ void f2_ff_accumulate(float2& Ah, float2& Al, float2 sh, float2 se, float2 dh, float2 dl) {
