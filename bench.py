@@ -239,7 +239,8 @@ def roofline_entry(name, pps, fp64_ops, fp32_ops, peak64, info64, peak32, info32
     traffic = {"traffic": prof.get(f"{name}_dram_bytes_per_launch"),
                "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the pair kernel and its "
                                "k_combine at 65,536 bodies (profiles/pair_kernels_65536.md, "
-                               "profiles/k_pairs_ff_65536.md)",
+                               "profiles/k_pairs_ff_65536.md; SPLIT_FF with the caches as the timed step "
+                               "leaves them, --cache-control none)",
                "kernel_ms_per_launch": ms}
     if name in fp32_ops:
         return {"bound": "fp32", "kernel": "k_pairs_ff (SPLIT_FF pair kernel) + k_combine",
