@@ -60,7 +60,10 @@ def _worker(rank, world, port, n_steps, out):
     replicas.finalize()
 
 
-def test_two_ranks_equal_the_single_process_driver():
+@pytest.mark.parametrize("world", [2, 4])
+def test_ranks_equal_the_single_process_driver(world):
+    """Two ranks, and four with sink blocks of uneven size (123 bodies: 31,
+    31, 31, 30; the all-gather pads them to the largest block)."""
     torch = pytest.importorskip("torch")
     import oracle
     s = _system()
@@ -69,7 +72,7 @@ def test_two_ranks_equal_the_single_process_driver():
     mp = torch.multiprocessing.get_context("spawn")
     q = mp.Queue()
     port = _free_port()
-    ps = [mp.Process(target=_worker, args=(r, 2, port, n_steps, q)) for r in range(2)]
+    ps = [mp.Process(target=_worker, args=(r, world, port, n_steps, q)) for r in range(world)]
     for p in ps:
         p.start()
     res = sorted((q.get(timeout=300) for _ in ps), key=lambda r: r[0])
@@ -77,7 +80,10 @@ def test_two_ranks_equal_the_single_process_driver():
         p.join(timeout=60)
         assert p.exitcode == 0
     blocks = [r[3] for r in res]
-    assert blocks[0][0] == 0 and blocks[0][1] == blocks[1][0] and blocks[1][1] == s.n
+    assert blocks[0][0] == 0 and blocks[-1][1] == s.n
+    assert all(blocks[k][1] == blocks[k + 1][0] for k in range(world - 1))
+    if world == 4:
+        assert len({hi - lo for lo, hi in blocks}) > 1
     for _, t, y, _, _ in res:
         assert t == ref["tl"][0]
         assert np.array_equal(y.view(np.uint64), ref["y0"].view(np.uint64))
