@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import csv
+import hashlib
 import io
 import json
 import os
@@ -94,7 +95,7 @@ def run_drift(args, local):
             out["forms"][name] = {"relative_energy_drift": drift, "every": every, "wall_s": wall,
                                   "final_max_rel_accel_err": float(rel.max()),
                                   "final_rms_rel_accel_err": float(np.sqrt(np.mean(rel ** 2))),
-                                  "final_state_sha": __import__("hashlib").sha256(y.tobytes()).hexdigest()[:16]}
+                                  "final_state_sha": hashlib.sha256(y.tobytes()).hexdigest()[:16]}
     print(json.dumps({"drift": out}))
 
 
