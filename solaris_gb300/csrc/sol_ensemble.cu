@@ -11,6 +11,8 @@
 // the system); the source table of an evaluation lives in shared memory.
 // FP64 mode follows the reference's operation order exactly, so each system
 // evolves as the single-system path (and the reference) would.
+#include <atomic>
+#include <mutex>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -311,10 +313,14 @@ int launch_ensemble(int grid, int block, size_t smem, cudaStream_t st, const Ens
 }
 
 int upload_tableau() {
-  static bool done[64] = {};
+  // once per device; contexts of several host threads may arrive together
+  static std::atomic<bool> done[64];
+  static std::mutex upload_mutex;
   int dev = 0;
   SOL_CUDA(cudaGetDevice(&dev));
-  if (dev >= 0 && dev < 64 && done[dev]) return SOL_OK;
+  if (dev >= 0 && dev < 64 && done[dev].load(std::memory_order_acquire)) return SOL_OK;
+  std::lock_guard<std::mutex> upload_lock(upload_mutex);
+  if (dev >= 0 && dev < 64 && done[dev].load(std::memory_order_relaxed)) return SOL_OK;
   int k[13] = {0};
   int idx[13][9] = {{0}};
   double a[13][9] = {{0}};
@@ -345,7 +351,7 @@ int upload_tableau() {
   SOL_CUDA(cudaMemcpyToSymbol(c_rk_k, k, sizeof(k)));
   SOL_CUDA(cudaMemcpyToSymbol(c_rk_idx, idx, sizeof(idx)));
   SOL_CUDA(cudaMemcpyToSymbol(c_rk_a, a, sizeof(a)));
-  if (dev >= 0 && dev < 64) done[dev] = true;
+  if (dev >= 0 && dev < 64) done[dev].store(true, std::memory_order_release);
   return SOL_OK;
 }
 

@@ -1431,24 +1431,27 @@ __global__ void __launch_bounds__(kFewSplitWarps * 32) k_pairs_few(ForceCtx fc, 
 // per SM avoid a nearly empty last round.
 static int split_chunk(const sol_ctx* c, int precision) {
   if (precision != SOL_PRECISION_SPLIT_FF) return kChunk;
-  static int sms[kMaxDevices], resident[kMaxDevices];
+  // per device, filled on first use; contexts of several host threads may
+  // race to fill them with the same values, hence the atomics
+  static std::atomic<int> sms[kMaxDevices], resident[kMaxDevices];
   const int dev = (c->device >= 0 && c->device < kMaxDevices) ? c->device : 0;
-  if (sms[dev] == 0) {
+  if (sms[dev].load(std::memory_order_relaxed) == 0) {
     int nsm = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 152;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_ff, kSinkBlock, 0) != cudaSuccess ||
         per_sm < 1)
       per_sm = 3;
-    resident[dev] = per_sm;
-    sms[dev] = nsm;
+    resident[dev].store(per_sm, std::memory_order_relaxed);
+    sms[dev].store(nsm, std::memory_order_release);
   }
   const long nb = (c->n + kSinkBlock - 1) / kSinkBlock;
-  const long nsm = sms[dev];
+  const long nsm = sms[dev].load(std::memory_order_acquire);
+  const long res = resident[dev].load(std::memory_order_relaxed);
   int best_ct = 1;
   double best = 1e300;
   for (int ct = kChunkTiles; ct >= 1; ct >>= 1) {
     const long ctas = nb * ((c->n + ct * kTile - 1) / (ct * kTile));
-    if (ctas < (long)resident[dev] * nsm) continue;
+    if (ctas < res * nsm) continue;
     const double cost = (double)((ctas + nsm - 1) / nsm) * (ct + 0.5);
     if (cost < best) {
       best = cost;
@@ -1489,18 +1492,22 @@ static int force_launch(sol_ctx* c, const ForceCtx& fc, const double* d_y, doubl
   // sinks with fewer sources than one producer tile (a few massive bodies and
   // many light ones) are cheaper with one thread per sink
   if (!split && c->cls.nm + c->cls.n_spl >= kFewTile) {
-    // per device: the SM count, once the wide kernel's shared-memory size is allowed
-    static int wide_sms[kMaxDevices];
+    // per device: the SM count, once the wide kernel's shared-memory size is
+    // allowed (contexts of several host threads may race to set it: the same
+    // values, hence an atomic published after the attribute call)
+    static std::atomic<int> wide_sms[kMaxDevices];
     const int dev = (c->device >= 0 && c->device < kMaxDevices) ? c->device : 0;
-    if (wide_sms[dev] == 0) {
+    int wsm = wide_sms[dev].load(std::memory_order_acquire);
+    if (wsm == 0) {
       int nsm = 0;
       SOL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
       SOL_CUDA(cudaFuncSetAttribute(k_gravity_ac_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWideSmem));
-      wide_sms[dev] = nsm;
+      wide_sms[dev].store(nsm, std::memory_order_release);
+      wsm = nsm;
     }
     // sinks per CTA: the fewest whole waves of two CTAs per SM, then the
     // cheapest of that and the next two wave counts
-    const int slots = kWideCtasPerSm * wide_sms[dev];
+    const int slots = kWideCtasPerSm * wsm;
     int spc = 0;
     {
       const int k0 = (nsink + slots * kWideSinks - 1) / (slots * kWideSinks);

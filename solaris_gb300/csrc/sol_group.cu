@@ -30,6 +30,8 @@
 // CTA that runs out raises SOL_DEV_TIMEOUT and an abort flag that makes every
 // other CTA leave at its next barrier.  (sol_set_wait_test lowers the limit
 // and can keep one CTA from arriving, so that tests reach this path.)
+#include <atomic>
+#include <mutex>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -826,10 +828,14 @@ __global__ void __launch_bounds__(kBlock) k_group_rkf78(GroupArgs P) {
 }
 
 int upload_group_tableau() {
-  static bool done[64] = {};
+  // once per device; contexts of several host threads may arrive together
+  static std::atomic<bool> done[64];
+  static std::mutex upload_mutex;
   int dev = 0;
   SOL_CUDA(cudaGetDevice(&dev));
-  if (dev >= 0 && dev < 64 && done[dev]) return SOL_OK;
+  if (dev >= 0 && dev < 64 && done[dev].load(std::memory_order_acquire)) return SOL_OK;
+  std::lock_guard<std::mutex> upload_lock(upload_mutex);
+  if (dev >= 0 && dev < 64 && done[dev].load(std::memory_order_relaxed)) return SOL_OK;
   int k[13] = {0};
   int idx[13][9] = {{0}};
   double a[13][9] = {{0}};
@@ -844,7 +850,7 @@ int upload_group_tableau() {
   SOL_CUDA(cudaMemcpyToSymbol(g_rk_k, k, sizeof(k)));
   SOL_CUDA(cudaMemcpyToSymbol(g_rk_idx, idx, sizeof(idx)));
   SOL_CUDA(cudaMemcpyToSymbol(g_rk_a, a, sizeof(a)));
-  if (dev >= 0 && dev < 64) done[dev] = true;
+  if (dev >= 0 && dev < 64) done[dev].store(true, std::memory_order_release);
   return SOL_OK;
 }
 

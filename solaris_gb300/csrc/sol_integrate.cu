@@ -9,6 +9,8 @@
 // decision (accept / shrink / grow, underflow, retry limit) is taken by a
 // one-thread control kernel that updates the device control block; the host
 // only reads the control block to decide whether to launch another attempt.
+#include <atomic>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -259,8 +261,11 @@ struct Rkf78Stage {
 
 const Rkf78Stage* rkf78_stages() {
   static Rkf78Stage st[13];
-  static bool init = false;
-  if (!init) {
+  // filled once; contexts of several host threads may arrive together
+  static std::atomic<bool> init{false};
+  static std::mutex init_mutex;
+  std::unique_lock<std::mutex> init_lock(init_mutex, std::defer_lock);
+  if (!init.load(std::memory_order_acquire) && (init_lock.lock(), !init.load(std::memory_order_relaxed))) {
     auto set = [](Rkf78Stage& s, std::initializer_list<int> idx, std::initializer_list<double> a) {
       s.k = (int)idx.size();
       int p = 0;
@@ -285,7 +290,7 @@ const Rkf78Stage* rkf78_stages() {
     set(st[12], {0, 3, 4, 5, 6, 7, 8, 9, 11},
         {-1777.0 / 4100.0, -341.0 / 164.0, 4496.0 / 1025.0, -289.0 / 82.0, 2193.0 / 4100.0, 51.0 / 82.0,
          33.0 / 164.0, 12.0 / 41.0, 1.0});
-    init = true;
+    init.store(true, std::memory_order_release);
   }
   return st;
 }
@@ -448,8 +453,11 @@ struct DpTab {
 const DpTab& dp_tab() {
   // DormandPrince::DormandPrince (DormandPrince.cpp:37-124)
   static DpTab T;
-  static bool init = false;
-  if (!init) {
+  // filled once; contexts of several host threads may arrive together
+  static std::atomic<bool> init{false};
+  static std::mutex init_mutex;
+  std::unique_lock<std::mutex> init_lock(init_mutex, std::defer_lock);
+  if (!init.load(std::memory_order_acquire) && (init_lock.lock(), !init.load(std::memory_order_relaxed))) {
     memset(&T, 0, sizeof(T));
     double sQ = sqrt(21.0);
     T.b[0] = 1.0 / 20.0; T.b[4] = 8.0 / 45.0; T.b[5] = 7.0 * (7.0 + sQ) / 360.0;
@@ -475,7 +483,7 @@ const DpTab& dp_tab() {
     T.a[7][6] = 7.0 * (5.0 - sQ) / 36.0;
     T.a[8][0] = 1.0 / 20.0; T.a[8][4] = 8.0 / 45.0; T.a[8][5] = 7.0 * (7.0 + sQ) / 360.0;
     T.a[8][6] = 7.0 * (7.0 - sQ) / 360.0;
-    init = true;
+    init.store(true, std::memory_order_release);
   }
   return T;
 }
@@ -715,8 +723,11 @@ int sol_integrate_partials_needed(int nv) { return grid_for(nv); }
 
 const Rkf78Table& sol_rkf78_table() {
   static Rkf78Table T;
-  static bool init = false;
-  if (!init) {
+  // filled once; contexts of several host threads may arrive together
+  static std::atomic<bool> init{false};
+  static std::mutex init_mutex;
+  std::unique_lock<std::mutex> init_lock(init_mutex, std::defer_lock);
+  if (!init.load(std::memory_order_acquire) && (init_lock.lock(), !init.load(std::memory_order_relaxed))) {
     memset(&T, 0, sizeof(T));
     const Rkf78Stage* st = rkf78_stages();
     for (int r = 1; r <= 12; ++r) {
@@ -726,7 +737,7 @@ const Rkf78Table& sol_rkf78_table() {
         T.a[r][q] = st[r].a[q];
       }
     }
-    init = true;
+    init.store(true, std::memory_order_release);
   }
   return T;
 }
