@@ -7,9 +7,12 @@ Cases (each holds a few hundred MB of device memory at most):
   fp64_wide       k_gravity_ac_wide: FP64 force, 16,384 self-gravitating bodies
   fp64_wide_65536 k_gravity_ac_wide: FP64 force at the bench size, 65,536 bodies
   split_65536     k_pairs<SPLIT> + k_combine: 65,536 bodies (bench size)
-  split_ff_65536  k_pairs<SPLIT_FF> + k_combine: 65,536 bodies (bench size)
-  split_ff_warp   k_pairs_few<SPLIT_FF>: float-float force, 4,096 bodies
-  split_ff_2d     k_pairs<SPLIT_FF> + k_combine: float-float force, 32,768 bodies
+  split_ff_65536  k_split_table + k_pairs_ff + k_combine: 65,536 bodies (bench size)
+  split_ff_warp   k_pairs_few<SPLIT_FF>: float-float force, one warp per sink,
+                  2,048 bodies (below the 4,096 where k_pairs_ff takes over)
+  split_ff_2d     k_pairs_ff + k_combine: float-float force, 32,768 bodies
+  potential       k_potential_pairs: the integrals' potential energy, 65,536
+                  bodies
   fp64_rate       k_fp64_rate<0,1,2>: the FP64 pipe throughput probe (DFMA,
                   DADD, DMUL chains), prints the rates and the SM clock
   fp32_rate       k_fp32_rate<0,1>: the FP32 pipe throughput probe (FFMA,
@@ -39,7 +42,7 @@ FORCE_CASES = {
     "fp64_wide_65536": (65536, abi.PRECISION_FP64),
     "split_65536": (65536, abi.PRECISION_SPLIT),
     "split_ff_65536": (65536, abi.PRECISION_SPLIT_FF),
-    "split_ff_warp": (4096, abi.PRECISION_SPLIT_FF),
+    "split_ff_warp": (2048, abi.PRECISION_SPLIT_FF),
     "split_ff_2d": (32768, abi.PRECISION_SPLIT_FF),
 }
 
@@ -50,6 +53,10 @@ def run(case: str) -> None:
         s = scenarios.config3(n=n)
         with engine.Context(s, precision=prec) as ctx:
             ctx.accel(0.0, s.y0)
+    elif case == "potential":
+        s = scenarios.config3(n=65536)
+        with engine.Context(s) as ctx:
+            ctx.integrals(s.y0)
     elif case == "fp64_rate":
         print(engine.fp64_pipe_rates(0))
     elif case == "fp32_rate":
