@@ -61,13 +61,18 @@ def run_drift(args, local):
     maximum / RMS relative acceleration error against the FP64 form evaluated
     at that state.  One JSON line."""
     import numpy as np
+
+    from solaris_gb300 import abi
+    forms = {"split_ff": abi.PRECISION_SPLIT_FF, "split": abi.PRECISION_SPLIT, "fp64": abi.PRECISION_FP64}
+    unknown = [f for f in args.drift_forms.split(",") if f not in forms]
+    if unknown:
+        raise SystemExit(f"bench.py: unknown --drift-forms {','.join(unknown)} (split_ff, split, fp64)")
     import torch
 
-    from solaris_gb300 import abi, build, engine, scenarios
+    from solaris_gb300 import build, engine, scenarios
     build.build()
     torch.cuda.set_device(local)
     s = scenarios.config3(n=args.n)
-    forms = {"split_ff": abi.PRECISION_SPLIT_FF, "split": abi.PRECISION_SPLIT, "fp64": abi.PRECISION_FP64}
     n_steps = args.drift_steps
     every = max(1, n_steps // 10)
     out = {"workload": WORKLOAD, "n_bodies": s.n, "integrator": "RungeKutta4", "h": s.h0, "steps": n_steps,

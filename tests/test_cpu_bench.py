@@ -68,3 +68,10 @@ def test_gpus_flag_must_match_the_world_size():
                        timeout=300, env=env)
     assert r.returncode != 0
     assert "WORLD_SIZE=3" in r.stderr
+
+
+def test_drift_mode_rejects_unknown_forms_before_any_device_work():
+    r = subprocess.run([sys.executable, "bench.py", "--drift-steps", "10", "--drift-forms", "split_ff,fp32"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode != 0
+    assert "unknown --drift-forms fp32" in r.stderr
