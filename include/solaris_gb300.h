@@ -315,8 +315,11 @@ int sol_check_events(sol_ctx* ctx, double ejection, double hit_centrum, double c
  * The 16 values of the reference's integrals record for the context's state
  * (or y0_or_null).  Up to 1,024 bodies the potential energy is the
  * reference's single running sum over ordered pairs, bit for bit (on the
- * host); above, the device sums per body and the host sums those, which may
- * differ in the last bits. */
+ * host); above, the device evaluates each unordered pair once (1/r from an
+ * FP32 seed and an FP64 Newton step) into per-CTA partials that the host adds
+ * in order: deterministic and within ~1e-13 relative of the exact sum, but
+ * not the reference's rounding.  Coincident bodies give +inf (NaN where one
+ * of the two masses is 0), as the reference's m_i m_j / 0. */
 int sol_integrals(sol_ctx* ctx, const double* y0_or_null, double integrals[16]);
 
 /* ---- output files: BinaryFileAdapter (Solaris/BinaryFileAdapter.cpp:107-219)
